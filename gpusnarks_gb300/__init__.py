@@ -1,0 +1,146 @@
+"""gpusnarks_gb300: GB300-native finite-field NTT behind the reference's
+``best_fft`` boundary (cuda/fft_kernel.h:24-25).
+
+This module is the host-side mirror of that interface for Python callers.  All
+work goes through the C ABI of the in-tree native library (include/
+gpusnarks_gb300.h); there is no CPU fallback.
+
+Element arrays use the reference layout: little-endian uint32 limbs per
+element (cuda/device_field.h:75), numpy shape ``(n, limbs)`` (``(n,)`` for
+the one-limb field) or the same bytes in a torch CUDA tensor of dtype int32.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._lib import GsnError, check, declared_symbols, library_path, load, u32p
+from .fields import BLS12_381, BY_ID, FIELDS, MNT4_753, MNT4_753_Q, P32, Field
+
+FORWARD, INVERSE, COSET_FORWARD, COSET_INVERSE = 0, 1, 2, 3
+DIRECTIONS = {"forward": FORWARD, "inverse": INVERSE, "coset_forward": COSET_FORWARD,
+              "coset_inverse": COSET_INVERSE}
+
+__all__ = ["Field", "P32", "BLS12_381", "MNT4_753", "MNT4_753_Q", "FIELDS", "BY_ID", "GsnError",
+           "FORWARD", "INVERSE", "COSET_FORWARD", "COSET_INVERSE", "load", "library_path",
+           "declared_symbols", "best_fft", "ntt", "root_of_unity", "field_of", "pointwise_mul",
+           "prepare", "launch_count"]
+
+
+def field_of(f) -> Field:
+    if isinstance(f, Field):
+        return f
+    if isinstance(f, str):
+        return FIELDS[f]
+    return BY_ID[int(f)]
+
+
+def _limbs(f: Field, x) -> np.ndarray | None:
+    if x is None:
+        return None
+    if isinstance(x, (int, np.integer)):
+        return f.to_limbs(int(x))
+    return np.ascontiguousarray(x, dtype=np.uint32).reshape(-1)[: f.limbs].copy()
+
+
+def root_of_unity(field, log_n: int) -> int:
+    f = field_of(field)
+    out = np.zeros(f.limbs, dtype=np.uint32)
+    check(load().gsn_root_of_unity(f.fid, log_n, u32p(out)))
+    return f.from_limbs(out)
+
+
+def prepare(field, log_n: int, omega=None) -> None:
+    f = field_of(field)
+    w = _limbs(f, omega)
+    check(load().gsn_prepare(f.fid, log_n, u32p(w)))
+
+
+def _log2_exact(n: int) -> int:
+    if n <= 0 or n & (n - 1):
+        raise ValueError(f"size {n} is not a power of two")
+    return n.bit_length() - 1
+
+
+def best_fft(a: np.ndarray, omg=None, *, field=None, direction=FORWARD, shift=None) -> np.ndarray:
+    """In-place transform of a host array, like ``best_fft(std::vector<FieldT>&, const FieldT&)``.
+
+    ``a``: numpy uint32 array of shape (n, limbs) (or (n,) for p32), modified in
+    place and returned.  ``omg``: the forward root (int or limbs); None = the
+    field's default root g^((p-1)/n).  ``field`` defaults from the limb count
+    (1 -> p32, 8 -> BLS12-381 r, 24 -> MNT4-753 r).
+    """
+    if not isinstance(a, np.ndarray) or a.dtype != np.uint32 or not a.flags.c_contiguous:
+        raise TypeError("best_fft expects a C-contiguous numpy uint32 array")
+    if field is None:
+        limbs = 1 if a.ndim == 1 else a.shape[1]
+        field = {1: P32, 8: BLS12_381, 24: MNT4_753}[limbs]
+    f = field_of(field)
+    n = a.size // f.limbs
+    log_n = _log2_exact(n)
+    w = _limbs(f, omg)
+    s = _limbs(f, shift)
+    check(load().gsn_ntt_host(f.fid, a.ctypes.data, log_n, u32p(w), int(direction), u32p(s)))
+    return a
+
+
+def _stream_handle(stream):
+    if stream is None:
+        import torch
+        return torch.cuda.current_stream().cuda_stream
+    if isinstance(stream, int):
+        return stream
+    return stream.cuda_stream
+
+
+def ntt(field, data, *, direction=FORWARD, omega=None, shift=None, stream=None, scratch=None):
+    """In-place transform of device data (a torch CUDA tensor, int32 storage).
+
+    Asynchronous on ``stream`` (default: torch's current stream).
+    """
+    f = field_of(field)
+    n = data.numel() // f.limbs
+    log_n = _log2_exact(n)
+    w = _limbs(f, omega)
+    s = _limbs(f, shift)
+    h = _stream_handle(stream)
+    lib = load()
+    if scratch is None:
+        check(lib.gsn_ntt(f.fid, data.data_ptr(), log_n, u32p(w), int(direction), u32p(s), h))
+    else:
+        check(lib.gsn_ntt_scratch(f.fid, data.data_ptr(), log_n, u32p(w), int(direction), u32p(s),
+                                  scratch.data_ptr(), h))
+    return data
+
+
+def pointwise_mul(field, a, b, *, stream=None):
+    f = field_of(field)
+    n = a.numel() // f.limbs
+    check(load().gsn_pointwise_mul(f.fid, a.data_ptr(), b.data_ptr(), n, _stream_handle(stream)))
+    return a
+
+
+def launch_count() -> int:
+    return int(load().gsn_kernel_launch_count())
+
+
+def to_device(arr: np.ndarray, device="cuda"):
+    """numpy uint32 limbs -> torch int32 CUDA tensor with the same bytes."""
+    import torch
+    return torch.from_numpy(np.ascontiguousarray(arr).view(np.int32)).to(device)
+
+
+def to_host(t) -> np.ndarray:
+    return t.cpu().numpy().view(np.uint32)
+
+
+def host_buffer(nbytes: int):
+    """Pinned host memory from the library (ctypes pointer, free with free_host_buffer)."""
+    p = ctypes.c_void_p()
+    check(load().gsn_host_alloc(ctypes.byref(p), nbytes))
+    return p
+
+
+def free_host_buffer(p) -> None:
+    check(load().gsn_host_free(p))

@@ -1,0 +1,284 @@
+// Device field arithmetic for the NTT path: Montgomery multiplication and
+// modular add/sub written as PTX carry chains.
+//
+// Replaces the reference's generic C++ limb loops (cuda/device_field_operators.h:
+// _add :104-117, _subtract :120-137, ciosMontgomeryMultiply :151-187,
+// Scalar::add/subtract/mul :190-214) with register-resident carry chains:
+//   * products:  mad.lo.cc / madc.lo.cc / mad.hi.cc / madc.hi.cc
+//   * add / sub: add.cc / addc, sub.cc / subc, then a branch-free select
+// and uses the correct CIOS constant -p^-1 mod 2^32 per field (the reference
+// hard-codes 0xFFFFFFFF, device_field_operators.h:47).
+//
+// Element layout is the reference's: uint32_t limbs, little-endian
+// (cuda/device_field.h:75).  All functions keep values canonical, in [0, p).
+// Montgomery products compute a*b*R^-1 mod p with R = 2^(32*N); the NTT
+// stores twiddles as w*R so that mont_mul(x, w*R) = x*w whatever
+// representation x is held in.
+#pragma once
+#include <cstdint>
+
+#include "fields_gen.h"
+
+namespace gsn {
+namespace ptx {
+
+// Every carry-chain step is its own volatile asm statement: the carry flag is
+// invisible to the compiler, and volatile keeps the statements of one chain in
+// program order.
+__device__ __forceinline__ void mad_lo_cc(uint32_t& d, uint32_t a, uint32_t b, uint32_t c) {
+  asm volatile("mad.lo.cc.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+}
+__device__ __forceinline__ void madc_lo_cc(uint32_t& d, uint32_t a, uint32_t b, uint32_t c) {
+  asm volatile("madc.lo.cc.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+}
+__device__ __forceinline__ void mad_hi_cc(uint32_t& d, uint32_t a, uint32_t b, uint32_t c) {
+  asm volatile("mad.hi.cc.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+}
+__device__ __forceinline__ void madc_hi_cc(uint32_t& d, uint32_t a, uint32_t b, uint32_t c) {
+  asm volatile("madc.hi.cc.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+}
+__device__ __forceinline__ void madc_hi(uint32_t& d, uint32_t a, uint32_t b, uint32_t c) {
+  asm volatile("madc.hi.u32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(c));
+}
+__device__ __forceinline__ void add_cc(uint32_t& d, uint32_t a, uint32_t b) {
+  asm volatile("add.cc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+}
+__device__ __forceinline__ void addc_cc(uint32_t& d, uint32_t a, uint32_t b) {
+  asm volatile("addc.cc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+}
+__device__ __forceinline__ void addc(uint32_t& d, uint32_t a, uint32_t b) {
+  asm volatile("addc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+}
+__device__ __forceinline__ void sub_cc(uint32_t& d, uint32_t a, uint32_t b) {
+  asm volatile("sub.cc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+}
+__device__ __forceinline__ void subc_cc(uint32_t& d, uint32_t a, uint32_t b) {
+  asm volatile("subc.cc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+}
+__device__ __forceinline__ void subc(uint32_t& d, uint32_t a, uint32_t b) {
+  asm volatile("subc.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+}
+__device__ __forceinline__ uint32_t mul_hi(uint32_t a, uint32_t b) {
+  uint32_t d;
+  asm("mul.hi.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+  return d;
+}
+
+}  // namespace ptx
+
+template <class P>
+struct Fe {
+  uint32_t l[P::N];
+};
+
+// ---------------------------------------------------------------------------
+// One-limb fields (p32).  p > 2^31, so there is no headroom for lazy sums:
+// every operation returns a canonical value.
+// ---------------------------------------------------------------------------
+template <class P>
+__device__ __forceinline__ uint32_t mul1(uint32_t a, uint32_t b) {
+  // Montgomery product with R = 2^32, subtractive form: m = lo * p^-1, so
+  // a*b - m*p has a zero low word and equals (hi - mulhi(m,p)) * 2^32,
+  // which lies in (-p*2^32, p*2^32).
+  constexpr uint32_t p = P::mod(0);
+  constexpr uint32_t pinv_pos = 0u - P::PINV;  // +p^-1 mod 2^32
+  uint32_t lo = a * b;
+  uint32_t hi = ptx::mul_hi(a, b);
+  uint32_t m = lo * pinv_pos;
+  uint32_t mh = ptx::mul_hi(m, p);
+  uint32_t r = hi - mh;
+  return (hi < mh) ? r + p : r;
+}
+template <class P>
+__device__ __forceinline__ uint32_t add1(uint32_t a, uint32_t b) {
+  constexpr uint32_t p = P::mod(0);
+  uint32_t t = p - b;  // in [1, p]
+  uint32_t r = a - t;
+  return (a < t) ? r + p : r;
+}
+template <class P>
+__device__ __forceinline__ uint32_t sub1(uint32_t a, uint32_t b) {
+  constexpr uint32_t p = P::mod(0);
+  uint32_t r = a - b;
+  return (a < b) ? r + p : r;
+}
+
+// ---------------------------------------------------------------------------
+// Multi-limb fields, one element per thread.
+// ---------------------------------------------------------------------------
+
+// r = a + b mod p.  Inputs canonical.
+template <class P>
+__device__ __forceinline__ void fe_add(Fe<P>& r, const Fe<P>& a, const Fe<P>& b) {
+  constexpr int N = P::N;
+  if constexpr (N == 1) {
+    r.l[0] = add1<P>(a.l[0], b.l[0]);
+  } else {
+    uint32_t s[N], d[N], c, mask;
+    ptx::add_cc(s[0], a.l[0], b.l[0]);
+#pragma unroll
+    for (int j = 1; j < N; ++j) ptx::addc_cc(s[j], a.l[j], b.l[j]);
+    ptx::addc(c, 0u, 0u);
+    ptx::sub_cc(d[0], s[0], P::mod(0));
+#pragma unroll
+    for (int j = 1; j < N; ++j) ptx::subc_cc(d[j], s[j], P::mod(j));
+    ptx::subc(mask, c, 0u);  // 0xFFFFFFFF iff s < p (no carry and a borrow)
+#pragma unroll
+    for (int j = 0; j < N; ++j) r.l[j] = (s[j] & mask) | (d[j] & ~mask);
+  }
+}
+
+// r = a - b mod p.  Inputs canonical.
+template <class P>
+__device__ __forceinline__ void fe_sub(Fe<P>& r, const Fe<P>& a, const Fe<P>& b) {
+  constexpr int N = P::N;
+  if constexpr (N == 1) {
+    r.l[0] = sub1<P>(a.l[0], b.l[0]);
+  } else {
+    uint32_t d[N], mask;
+    ptx::sub_cc(d[0], a.l[0], b.l[0]);
+#pragma unroll
+    for (int j = 1; j < N; ++j) ptx::subc_cc(d[j], a.l[j], b.l[j]);
+    ptx::subc(mask, 0u, 0u);  // 0xFFFFFFFF iff a < b
+    ptx::add_cc(r.l[0], d[0], P::mod(0) & mask);
+#pragma unroll
+    for (int j = 1; j < N - 1; ++j) ptx::addc_cc(r.l[j], d[j], P::mod(j) & mask);
+    ptx::addc(r.l[N - 1], d[N - 1], P::mod(N - 1) & mask);
+  }
+}
+
+// One CIOS reduction step on the accumulator t[0..N+1]: m = t0 * (-p^-1),
+// t += m*p (t0 becomes 0), then t >>= 32.
+template <class P>
+__device__ __forceinline__ void cios_reduce_step(uint32_t (&t)[P::N + 2]) {
+  constexpr int N = P::N;
+  const uint32_t m = t[0] * P::PINV;
+  ptx::mad_lo_cc(t[0], m, P::mod(0), t[0]);
+#pragma unroll
+  for (int j = 1; j < N; ++j) ptx::madc_lo_cc(t[j], m, P::mod(j), t[j]);
+  ptx::addc_cc(t[N], t[N], 0u);
+  ptx::addc(t[N + 1], t[N + 1], 0u);
+  ptx::mad_hi_cc(t[1], m, P::mod(0), t[1]);
+#pragma unroll
+  for (int j = 1; j < N; ++j) ptx::madc_hi_cc(t[j + 1], m, P::mod(j), t[j + 1]);
+  ptx::addc(t[N + 1], t[N + 1], 0u);
+#pragma unroll
+  for (int j = 0; j <= N; ++j) t[j] = t[j + 1];
+  t[N + 1] = 0u;
+}
+
+// r = a * b * R^-1 mod p (CIOS, Koc-Acar-Kaliski), lo and hi partial
+// products in two carry chains per row.  Inputs canonical; output canonical.
+template <class P>
+__device__ __forceinline__ void fe_mul(Fe<P>& r, const Fe<P>& a, const Fe<P>& b) {
+  constexpr int N = P::N;
+  if constexpr (N == 1) {
+    r.l[0] = mul1<P>(a.l[0], b.l[0]);
+  } else {
+    uint32_t t[N + 2];
+    {  // row 0: t = a * b0
+      const uint32_t bi = b.l[0];
+#pragma unroll
+      for (int j = 0; j < N; ++j) t[j] = a.l[j] * bi;
+      ptx::mad_hi_cc(t[1], a.l[0], bi, t[1]);
+#pragma unroll
+      for (int j = 1; j < N - 1; ++j) ptx::madc_hi_cc(t[j + 1], a.l[j], bi, t[j + 1]);
+      ptx::madc_hi(t[N], a.l[N - 1], bi, 0u);
+      t[N + 1] = 0u;
+      cios_reduce_step<P>(t);
+    }
+#pragma unroll
+    for (int i = 1; i < N; ++i) {
+      const uint32_t bi = b.l[i];
+      ptx::mad_lo_cc(t[0], a.l[0], bi, t[0]);
+#pragma unroll
+      for (int j = 1; j < N; ++j) ptx::madc_lo_cc(t[j], a.l[j], bi, t[j]);
+      ptx::addc_cc(t[N], t[N], 0u);
+      ptx::addc(t[N + 1], 0u, 0u);
+      ptx::mad_hi_cc(t[1], a.l[0], bi, t[1]);
+#pragma unroll
+      for (int j = 1; j < N; ++j) ptx::madc_hi_cc(t[j + 1], a.l[j], bi, t[j + 1]);
+      ptx::addc(t[N + 1], t[N + 1], 0u);
+      cios_reduce_step<P>(t);
+    }
+    // t < 2p: one conditional subtraction
+    uint32_t d[N], mask;
+    ptx::sub_cc(d[0], t[0], P::mod(0));
+#pragma unroll
+    for (int j = 1; j < N; ++j) ptx::subc_cc(d[j], t[j], P::mod(j));
+    ptx::subc(mask, t[N], 0u);  // 0xFFFFFFFF iff t < p
+#pragma unroll
+    for (int j = 0; j < N; ++j) r.l[j] = (t[j] & mask) | (d[j] & ~mask);
+  }
+}
+
+// Montgomery form helpers (device): x*R and x*R^-1.
+template <class P>
+__device__ __forceinline__ void fe_to_mont(Fe<P>& r, const Fe<P>& a) {
+  Fe<P> r2;
+#pragma unroll
+  for (int j = 0; j < P::N; ++j) r2.l[j] = P::r2(j);
+  fe_mul<P>(r, a, r2);
+}
+
+template <class P>
+__device__ __forceinline__ void fe_set_one_mont(Fe<P>& r) {
+#pragma unroll
+  for (int j = 0; j < P::N; ++j) r.l[j] = P::r1(j);
+}
+
+// --- loads and stores (16-byte vectors when the element allows) -------------
+template <class P>
+__device__ __forceinline__ void fe_load(Fe<P>& r, const uint32_t* p) {
+  constexpr int N = P::N;
+  if constexpr (N % 4 == 0) {
+    const uint4* q = reinterpret_cast<const uint4*>(p);
+#pragma unroll
+    for (int k = 0; k < N / 4; ++k) {
+      uint4 v = q[k];
+      r.l[4 * k + 0] = v.x;
+      r.l[4 * k + 1] = v.y;
+      r.l[4 * k + 2] = v.z;
+      r.l[4 * k + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.l[k] = p[k];
+  }
+}
+
+// Load that bypasses L1 (ld.global.cg): used for data another CTA of the same
+// launch may have written (the batched kernel reads earlier passes' output).
+template <class P>
+__device__ __forceinline__ void fe_load_cg(Fe<P>& r, const uint32_t* p) {
+  constexpr int N = P::N;
+  if constexpr (N % 4 == 0) {
+    const uint4* q = reinterpret_cast<const uint4*>(p);
+#pragma unroll
+    for (int k = 0; k < N / 4; ++k) {
+      uint4 v = __ldcg(q + k);
+      r.l[4 * k + 0] = v.x;
+      r.l[4 * k + 1] = v.y;
+      r.l[4 * k + 2] = v.z;
+      r.l[4 * k + 3] = v.w;
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < N; ++k) r.l[k] = __ldcg(p + k);
+  }
+}
+
+template <class P>
+__device__ __forceinline__ void fe_store(uint32_t* p, const Fe<P>& a) {
+  constexpr int N = P::N;
+  if constexpr (N % 4 == 0) {
+    uint4* q = reinterpret_cast<uint4*>(p);
+#pragma unroll
+    for (int k = 0; k < N / 4; ++k) q[k] = make_uint4(a.l[4 * k], a.l[4 * k + 1], a.l[4 * k + 2], a.l[4 * k + 3]);
+  } else {
+#pragma unroll
+    for (int k = 0; k < N; ++k) p[k] = a.l[k];
+  }
+}
+
+}  // namespace gsn

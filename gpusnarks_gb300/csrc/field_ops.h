@@ -1,0 +1,43 @@
+// Type-erased per-field operations: kernel launchers (defined in the
+// per-field translation units ntt_f_*.cu) and host arithmetic helpers.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "ntt_common.h"
+
+namespace gsn {
+
+struct FieldOps {
+  int id;
+  int limbs;
+  int two_adicity;
+  int max_log_n;       // largest supported transform (2-adicity and memory)
+  int default_tw_log;  // size of the shared default twiddle table
+  uint32_t generator;  // multiplicative generator (a quadratic non-residue)
+  // device
+  cudaError_t (*pass)(const PassArgs& A, int block, cudaStream_t s);
+  cudaError_t (*powers)(uint32_t* out, uint64_t count, const uint32_t* base_canon, cudaStream_t s);
+  cudaError_t (*pointwise)(uint32_t* a, const uint32_t* b, uint64_t n, cudaStream_t s);
+  cudaError_t (*batch)(const BatchJob* jobs_dev, const uint64_t* work_dev, uint64_t nwork,
+                       uint32_t* counters_dev, uint32_t* status_dev, int grid, int block, size_t smem,
+                       cudaStream_t s);
+  int (*batch_occupancy)(int block, size_t smem);
+  // host (canonical limbs in/out)
+  void (*root)(int log_n, uint32_t* out);
+  bool (*is_primitive)(const uint32_t* w, int log_n);
+  bool (*is_canonical)(const uint32_t* x);
+  void (*inv)(const uint32_t* x, uint32_t* out);
+  void (*to_mont)(const uint32_t* x, uint32_t* out);
+  void (*pow)(const uint32_t* x, uint64_t e, uint32_t* out);
+  void (*modulus)(uint32_t* out);
+};
+
+extern const FieldOps kOpsP32;
+extern const FieldOps kOpsBLS12_381;
+extern const FieldOps kOpsMNT4_753;
+
+const FieldOps* field_ops(int field);
+
+}  // namespace gsn

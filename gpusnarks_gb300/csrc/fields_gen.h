@@ -3,6 +3,8 @@
 #pragma once
 #include <cstdint>
 
+#include "gsn_compat.h"
+
 namespace gsn {
 
 // p32: 32-bit modulus, 1 limb(s), 2-adicity 30, generator 5

@@ -1,0 +1,361 @@
+// NTT kernels, templated on the field.  Included by one .cu per field so the
+// fields compile in parallel.
+//
+// Replaces cuda_fft (cuda/fft_kernel.cu:79-142).  The reference launches 1280
+// threads that each run a 1024-term direct sum and a 64-point radix-2 loop in
+// local memory (O(n * 1024) products); here each pass is a radix-2^r
+// sub-transform of a shared-memory tile (see ntt_common.h for the
+// decomposition), so a transform costs (n/2) log2 n products plus one
+// twiddle product per element per pass boundary.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "arith.cuh"
+#include "ntt_common.h"
+
+namespace gsn {
+
+__device__ __forceinline__ uint32_t bitrev_bits(uint32_t x, int bits) {
+  return bits == 0 ? 0u : (__brev(x) >> (32 - bits));
+}
+
+// Table index of w_n^e (e in units of the transform's own root).
+__device__ __forceinline__ uint64_t tw_index(int tw_log, int log_n, int inverse, uint64_t e) {
+  const uint64_t size = (uint64_t)1 << tw_log;
+  uint64_t idx = e << (tw_log - log_n);
+  if (inverse) idx = (size - idx) & (size - 1);
+  return idx;
+}
+
+template <class P>
+__device__ __forceinline__ void tw_load(Fe<P>& w, const uint32_t* tw, uint64_t idx) {
+  fe_load<P>(w, tw + idx * P::N);
+}
+
+// Mixed-radix digit reversal of the last pass's "rest" prefix index
+// (digits k_1..k_{P-2}, row-major) into the output offset
+// k_1 + n_1 k_2 + ... (before the final multiplication by n_0).
+__device__ __forceinline__ uint64_t rest_offset(uint64_t rest, int npass, const int* radix_log) {
+  uint64_t off = 0;
+  int shift_before[kMaxPasses];
+  int acc = 0;
+  for (int i = 1; i < npass - 1; ++i) {
+    shift_before[i] = acc;
+    acc += radix_log[i];
+  }
+  for (int i = npass - 2; i >= 1; --i) {
+    const uint64_t digit = rest & (((uint64_t)1 << radix_log[i]) - 1);
+    rest >>= radix_log[i];
+    off += digit << shift_before[i];
+  }
+  return off;
+}
+
+// One tile of one pass.  `sm` holds 2^(log_r + log_j) elements.
+template <class P>
+__device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
+  constexpr int N = P::N;
+  const int lr = A.log_r, lj = A.log_j;
+  const int R = 1 << lr, J = 1 << lj;
+  const int tid = threadIdx.x, nthr = blockDim.x;
+
+  // --- tile geometry -------------------------------------------------------
+  uint64_t base = 0;     // non-last: first element of the tile
+  uint64_t jbase = 0;    // non-last: first suffix index j'
+  uint64_t rowpre = 0;   // last: prefix_lin of row 0 = (k0_first << (outer_log - lo0)) + rest
+  uint64_t obase = 0;    // last: output offset of row 0 (k_0 = k0_first, k = 0)
+  int lo0 = 0;           // last: log2 n_0 (0 for a single pass)
+  if (!A.last) {
+    const int per_prefix_log = A.log_inner - lj;
+    const uint64_t prefix = tile >> per_prefix_log;
+    const uint64_t jb = tile & (((uint64_t)1 << per_prefix_log) - 1);
+    jbase = jb << lj;
+    base = (prefix << (lr + A.log_inner)) + jbase;
+  } else {
+    lo0 = (A.npass == 1) ? 0 : A.radix_log[0];
+    const int k0b_log = lo0 - lj;
+    const uint64_t k0b = tile & (((uint64_t)1 << k0b_log) - 1);
+    const uint64_t rest = tile >> k0b_log;
+    const uint64_t k0 = k0b << lj;
+    rowpre = (k0 << (A.log_outer - lo0)) + rest;
+    obase = k0 + (rest_offset(rest, A.npass, A.radix_log) << lo0);
+  }
+
+  Fe<P> pre_c;
+  if (A.first && A.has_pre_const) {
+#pragma unroll
+    for (int w = 0; w < N; ++w) pre_c.l[w] = A.pre_const[w];
+  }
+
+  // --- load ----------------------------------------------------------------
+  for (int e = tid; e < R * J; e += nthr) {
+    int k, jj;
+    uint64_t gpos;
+    if (!A.last) {
+      k = e >> lj;
+      jj = e & (J - 1);
+      gpos = base + ((uint64_t)k << A.log_inner) + jj;
+    } else {
+      jj = e >> lr;
+      k = e & (R - 1);
+      gpos = ((rowpre + ((uint64_t)jj << (A.log_outer - lo0))) << lr) + k;
+    }
+    Fe<P> x;
+    fe_load_cg<P>(x, A.src + gpos * N);
+    if (A.first) {
+      if (A.pre_table) {
+        Fe<P> s;
+        fe_load<P>(s, A.pre_table + gpos * N);
+        fe_mul<P>(x, x, s);
+      }
+      if (A.has_pre_const) fe_mul<P>(x, x, pre_c);
+    }
+    fe_store<P>(sm + ((uint64_t)((k << lj) + jj)) * N, x);
+  }
+  __syncthreads();
+
+  // --- radix-2 DIF stages (natural in, bit-reversed out within the tile) ---
+  for (int s = 0; s < lr; ++s) {
+    const int log_half = lr - 1 - s;
+    for (int b = tid; b < (R >> 1) * J; b += nthr) {
+      const int jj = b & (J - 1);
+      const int bb = b >> lj;
+      const int i = bb & ((1 << log_half) - 1);
+      const int g = bb >> log_half;
+      const int u = (g << (log_half + 1)) + i;
+      const int v = u + (1 << log_half);
+      Fe<P> x, y, sum, dif;
+      fe_load<P>(x, sm + ((u << lj) + jj) * N);
+      fe_load<P>(y, sm + ((v << lj) + jj) * N);
+      fe_add<P>(sum, x, y);
+      fe_sub<P>(dif, x, y);
+      if (i != 0) {
+        Fe<P> w;
+        const uint64_t e = ((uint64_t)i << s) << (A.log_n - lr);
+        tw_load<P>(w, A.tw, tw_index(A.tw_log, A.log_n, A.inverse, e));
+        fe_mul<P>(dif, dif, w);
+      }
+      fe_store<P>(sm + ((u << lj) + jj) * N, sum);
+      fe_store<P>(sm + ((v << lj) + jj) * N, dif);
+    }
+    __syncthreads();
+  }
+
+  // --- twiddle and store ---------------------------------------------------
+  for (int e = tid; e < R * J; e += nthr) {
+    const int k = e >> lj;
+    const int jj = e & (J - 1);
+    const uint32_t q = bitrev_bits((uint32_t)k, lr);
+    Fe<P> x;
+    fe_load<P>(x, sm + ((q << lj) + jj) * N);
+    if (!A.last) {
+      const uint64_t jp = jbase + jj;
+      const uint64_t ex = (jp * (uint64_t)k) << A.log_outer;
+      if (ex != 0) {
+        Fe<P> w;
+        tw_load<P>(w, A.tw, tw_index(A.tw_log, A.log_n, A.inverse, ex));
+        fe_mul<P>(x, x, w);
+      }
+      fe_store<P>(A.dst + (base + ((uint64_t)k << A.log_inner) + jj) * N, x);
+    } else {
+      const uint64_t opos = obase + jj + ((uint64_t)k << A.log_outer);
+      if (A.post_table) {
+        Fe<P> s;
+        fe_load<P>(s, A.post_table + opos * N);
+        fe_mul<P>(x, x, s);
+      }
+      fe_store<P>(A.dst + opos * N, x);
+    }
+  }
+  __syncthreads();
+}
+
+template <class P>
+__global__ void ntt_pass_kernel(PassArgs A) {
+  extern __shared__ uint4 gsn_smem[];
+  uint32_t* sm = reinterpret_cast<uint32_t*>(gsn_smem);
+  for (uint64_t t = blockIdx.x; t < A.tiles; t += gridDim.x) ntt_tile<P>(A, t, sm);
+}
+
+// out[e] = base^e * R (Montgomery form) for e in [0, count).  `base` is
+// canonical.  Each thread produces kPowChunk consecutive powers: one
+// square-and-multiply for the first, then one product per entry.
+constexpr int kPowChunk = 32;
+
+template <class P>
+__global__ void gen_powers_kernel(uint32_t* out, uint64_t count, Fe<P> base) {
+  const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const uint64_t e0 = t * kPowChunk;
+  if (e0 >= count) return;
+  Fe<P> bm, acc;
+  fe_to_mont<P>(bm, base);
+  fe_set_one_mont<P>(acc);
+  // acc = bm^e0 (left to right over the bits of e0)
+  if (e0 != 0) {
+    for (int bit = 63 - __clzll((long long)e0); bit >= 0; --bit) {
+      fe_mul<P>(acc, acc, acc);
+      if ((e0 >> bit) & 1) fe_mul<P>(acc, acc, bm);
+    }
+  }
+  const uint64_t end = (e0 + kPowChunk < count) ? e0 + kPowChunk : count;
+  for (uint64_t e = e0; e < end; ++e) {
+    fe_store<P>(out + e * P::N, acc);
+    fe_mul<P>(acc, acc, bm);
+  }
+}
+
+// a[i] = a[i] * b[i] mod p (canonical in, canonical out): two Montgomery
+// products, the second by R^2.
+template <class P>
+__global__ void pointwise_mul_kernel(uint32_t* a, const uint32_t* b, uint64_t n) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    Fe<P> x, y, r;
+    fe_load<P>(x, a + i * P::N);
+    fe_load<P>(y, b + i * P::N);
+    fe_mul<P>(r, x, y);
+    fe_to_mont<P>(r, r);
+    fe_store<P>(a + i * P::N, r);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Batched transforms: one persistent launch over many jobs.
+//
+// work[t] = job << 32 | pass << 28 | tile, ordered by pass level (every
+// level-0 tile of every job, then level 1, ...).  CTAs claim tickets in order
+// from counters[0]; a tile of pass p > 0 first waits until
+// counters[1 + job*kMaxPasses + p-1] reaches the tile count of pass p-1 of
+// that job.  Those tiles hold smaller tickets, so they are already claimed by
+// running CTAs that wait only on even smaller tickets: the waits always end.
+// Each wait is still bounded (kWaitBudgetCycles); on expiry the CTA records
+// GSN timeout in *status and carries on, so the launch always terminates.
+// ---------------------------------------------------------------------------
+constexpr long long kWaitBudgetCycles = 8LL * 1000 * 1000 * 1000;  // ~4 s at 2 GHz
+
+__device__ __forceinline__ uint32_t ld_volatile_u32(const uint32_t* p) {
+  uint32_t v;
+  asm volatile("ld.volatile.global.u32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
+
+__device__ __forceinline__ void job_pass_args(PassArgs& A, const BatchJob& J, int pass) {
+  int outer = 0;
+  for (int i = 0; i < pass; ++i) outer += J.radix_log[i];
+  A.first = pass == 0;
+  A.last = pass == J.npass - 1;
+  A.src = A.first ? J.data : J.scratch;
+  A.dst = A.last ? J.data : J.scratch;
+  A.tw = J.tw;
+  A.tw_log = J.tw_log;
+  A.log_n = J.log_n;
+  A.log_r = J.radix_log[pass];
+  A.log_outer = outer;
+  A.log_inner = J.log_n - outer - J.radix_log[pass];
+  A.log_j = J.log_j[pass];
+  A.inverse = J.inverse;
+  A.npass = J.npass;
+  for (int i = 0; i < kMaxPasses; ++i) A.radix_log[i] = J.radix_log[i];
+  A.pre_table = A.first ? J.pre_table : nullptr;
+  A.post_table = A.last ? J.post_table : nullptr;
+  A.has_pre_const = A.first ? J.has_pre_const : 0;
+  if (A.has_pre_const)
+    for (int i = 0; i < kMaxLimbs; ++i) A.pre_const[i] = J.pre_const[i];
+  A.tiles = (uint64_t)1 << (J.log_n - A.log_r - A.log_j);
+}
+
+template <class P>
+__global__ void batch_kernel(const BatchJob* __restrict__ jobs, const uint64_t* __restrict__ work,
+                             uint64_t nwork, uint32_t* counters, uint32_t* status) {
+  extern __shared__ uint4 gsn_smem[];
+  uint32_t* sm = reinterpret_cast<uint32_t*>(gsn_smem);
+  __shared__ uint32_t s_ticket;
+  __shared__ PassArgs s_args;
+  for (;;) {
+    if (threadIdx.x == 0) s_ticket = atomicAdd(&counters[0], 1u);
+    __syncthreads();
+    const uint32_t t = s_ticket;
+    if (t >= nwork) return;
+    const uint64_t w = work[t];
+    const uint32_t job = (uint32_t)(w >> 32);
+    const int pass = (int)((w >> 28) & 0xF);
+    const uint64_t tile = w & 0x0FFFFFFFull;
+    if (threadIdx.x == 0) {
+      const BatchJob& J = jobs[job];
+      job_pass_args(s_args, J, pass);
+      if (pass > 0) {
+        const uint32_t need = (uint32_t)((uint64_t)1 << (J.log_n - J.radix_log[pass - 1] - J.log_j[pass - 1]));
+        const uint32_t* cnt = &counters[1 + (uint64_t)job * kMaxPasses + pass - 1];
+        const long long start = clock64();
+        while (ld_volatile_u32(cnt) < need) {
+          if (clock64() - start > kWaitBudgetCycles) {
+            atomicExch(status, 8u);  // GSN_ERR_TIMEOUT
+            break;
+          }
+          __nanosleep(256);
+        }
+        __threadfence();
+      }
+    }
+    __syncthreads();
+    PassArgs A = s_args;
+    ntt_tile<P>(A, tile, sm);  // ends with __syncthreads()
+    if (threadIdx.x == 0) {
+      __threadfence();
+      atomicAdd(&counters[1 + (uint64_t)job * kMaxPasses + pass], 1u);
+    }
+  }
+}
+
+// --- host-side launchers, instantiated per field ---------------------------
+template <class P>
+struct Kernels {
+  static cudaError_t pass(const PassArgs& A, int block, cudaStream_t s) {
+    const size_t smem = ((size_t)1 << (A.log_r + A.log_j)) * P::N * sizeof(uint32_t);
+    auto k = ntt_pass_kernel<P>;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    const uint64_t grid = A.tiles < (1u << 20) ? A.tiles : (1u << 20);
+    k<<<(unsigned)grid, block, smem, s>>>(A);
+    return cudaGetLastError();
+  }
+  static cudaError_t powers(uint32_t* out, uint64_t count, const uint32_t* base_canon, cudaStream_t s) {
+    Fe<P> b;
+    for (int i = 0; i < P::N; ++i) b.l[i] = base_canon[i];
+    const uint64_t threads = (count + kPowChunk - 1) / kPowChunk;
+    const int block = 128;
+    gen_powers_kernel<P><<<(unsigned)((threads + block - 1) / block), block, 0, s>>>(out, count, b);
+    return cudaGetLastError();
+  }
+  static cudaError_t batch(const BatchJob* jobs_dev, const uint64_t* work_dev, uint64_t nwork,
+                           uint32_t* counters_dev, uint32_t* status_dev, int grid, int block, size_t smem,
+                           cudaStream_t s) {
+    auto k = batch_kernel<P>;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    k<<<grid, block, smem, s>>>(jobs_dev, work_dev, nwork, counters_dev, status_dev);
+    return cudaGetLastError();
+  }
+  static int batch_occupancy(int block, size_t smem) {
+    auto k = batch_kernel<P>;
+    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    int nb = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, block, smem) != cudaSuccess) return 0;
+    return nb;
+  }
+  static cudaError_t pointwise(uint32_t* a, const uint32_t* b, uint64_t n, cudaStream_t s) {
+    const int block = 256;
+    uint64_t grid = (n + block - 1) / block;
+    if (grid > 152 * 64) grid = 152 * 64;
+    pointwise_mul_kernel<P><<<(unsigned)grid, block, 0, s>>>(a, b, n);
+    return cudaGetLastError();
+  }
+};
+
+}  // namespace gsn

@@ -1,0 +1,518 @@
+// Runtime and C ABI for single transforms.
+//
+// Replaces the host launcher best_fft (cuda/fft_kernel.cu:144-174): that one
+// prints, asserts n == 2^16, ignores omg, cudaMallocs two buffers per call
+// that it never frees, launches one fixed <<<5,256>>> grid and exits the
+// process on a launch error.  Here a call validates its arguments, resolves
+// device-resident twiddle tables (built once per (field, root) and cached),
+// enqueues one kernel per pass on the caller's stream and returns an error
+// code on any failure.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <atomic>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "gpusnarks_gb300.h"
+#include "runtime.h"
+
+namespace gsn {
+
+// ---------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------
+static thread_local std::string t_error;
+
+int set_error(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  t_error = buf;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char* what) {
+  return set_error(GSN_ERR_CUDA, "%s failed: %s (%d)", what, cudaGetErrorString(e), (int)e);
+}
+
+static std::atomic<uint64_t> g_launches{0};
+void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+const FieldOps* field_ops(int field) {
+  switch (field) {
+    case GSN_P32: return &kOpsP32;
+    case GSN_BLS12_381_FR: return &kOpsBLS12_381;
+    case GSN_MNT4753_FR: return &kOpsMNT4_753;
+    default: return nullptr;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// device allocations
+// ---------------------------------------------------------------------------
+int dev_alloc(void** p, size_t bytes) {
+  cudaError_t e = cudaMalloc(p, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return set_error(GSN_ERR_NOMEM, "cudaMalloc(%zu) failed: %s", bytes, cudaGetErrorString(e));
+  }
+  return GSN_OK;
+}
+
+void dev_free(void* p) {
+  if (p) cudaFree(p);
+}
+
+// ---------------------------------------------------------------------------
+// plans
+// ---------------------------------------------------------------------------
+struct FieldLimits {
+  int max_r, target_j, max_block;
+};
+
+static FieldLimits limits_of(const FieldOps& F) {
+  switch (F.id) {
+    case GSN_P32: return {11, 3, 512};
+    case GSN_BLS12_381_FR: return {9, 2, 256};
+    default: return {8, 1, 128};
+  }
+}
+
+size_t plan_smem_bytes(const FieldOps& F, const Plan& p, int pass) {
+  return ((size_t)1 << (p.radix_log[pass] + p.log_j[pass])) * F.limbs * sizeof(uint32_t);
+}
+
+bool plan_valid(const FieldOps& F, const Plan& p) {
+  if (p.npass < 1 || p.npass > kMaxPasses) return false;
+  int sum = 0;
+  for (int i = 0; i < p.npass; ++i) {
+    if (p.radix_log[i] < 0 || p.log_j[i] < 0) return false;
+    sum += p.radix_log[i];
+    if (p.block[i] < 32 || p.block[i] > 1024 || (p.block[i] & 31)) return false;
+    if (plan_smem_bytes(F, p, i) > 200 * 1024) return false;
+  }
+  if (sum != p.log_n) return false;
+  for (int i = 0; i < p.npass; ++i) {
+    const bool last = i == p.npass - 1;
+    int inner = 0;
+    for (int k = i + 1; k < p.npass; ++k) inner += p.radix_log[k];
+    if (!last && p.log_j[i] > inner) return false;
+    if (last && p.npass > 1 && p.log_j[i] > p.radix_log[0]) return false;
+    if (last && p.npass == 1 && p.log_j[i] != 0) return false;
+  }
+  return true;
+}
+
+Plan make_plan(const FieldOps& F, int log_n, int max_r, int target_j, int max_block) {
+  Plan p;
+  p.log_n = log_n;
+  p.npass = std::max(1, (log_n + max_r - 1) / max_r);
+  if (p.npass > kMaxPasses) p.npass = kMaxPasses;
+  const int base = log_n / p.npass, extra = log_n % p.npass;
+  for (int i = 0; i < p.npass; ++i) p.radix_log[i] = base + (i < extra ? 1 : 0);
+  for (int i = 0; i < p.npass; ++i) {
+    const bool last = i == p.npass - 1;
+    int inner = 0;
+    for (int k = i + 1; k < p.npass; ++k) inner += p.radix_log[k];
+    int lj = last ? (p.npass == 1 ? 0 : std::min(target_j, p.radix_log[0])) : std::min(target_j, inner);
+    p.log_j[i] = lj;
+    int work = std::max(1, (1 << (p.radix_log[i] + lj)) / 2);
+    int blk = 32;
+    while (blk < max_block && blk < work) blk *= 2;
+    p.block[i] = blk;
+  }
+  (void)F;
+  return p;
+}
+
+static std::mutex g_plan_mu;
+static std::map<std::pair<int, int>, Plan> g_tuned;
+
+void set_tuned_plan(int field, int log_n, const Plan& p) {
+  std::lock_guard<std::mutex> g(g_plan_mu);
+  g_tuned[{field, log_n}] = p;
+}
+void clear_tuned_plans() {
+  std::lock_guard<std::mutex> g(g_plan_mu);
+  g_tuned.clear();
+}
+bool get_tuned_plan(int field, int log_n, Plan* out) {
+  std::lock_guard<std::mutex> g(g_plan_mu);
+  auto it = g_tuned.find({field, log_n});
+  if (it == g_tuned.end()) return false;
+  *out = it->second;
+  return true;
+}
+
+Plan plan_for(const FieldOps& F, int log_n) {
+  Plan p;
+  if (get_tuned_plan(F.id, log_n, &p) && plan_valid(F, p)) return p;
+  FieldLimits L = limits_of(F);
+  return make_plan(F, log_n, L.max_r, L.target_j, L.max_block);
+}
+
+// ---------------------------------------------------------------------------
+// twiddle / coset table cache
+// ---------------------------------------------------------------------------
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+struct TableCache {
+  std::mutex mu;
+  // (field, tw_log, root limbs) -> powers of the root
+  std::map<std::tuple<int, int, std::string>, DevBuf> powers;
+  std::map<cudaStream_t, DevBuf> scratch;
+  cudaStream_t gen_stream = nullptr;
+};
+
+static TableCache& cache() {
+  static TableCache* c = new TableCache();  // never destroyed: outlives static teardown order
+  return *c;
+}
+
+static std::string limbs_key(const uint32_t* x, int n) {
+  return std::string(reinterpret_cast<const char*>(x), sizeof(uint32_t) * n);
+}
+
+// Returns a cached table of base^e * R for e in [0, 2^log_count); builds it
+// on first use.  Caller holds no lock.
+static int powers_table(const FieldOps& F, const uint32_t* base, int log_count, const uint32_t** out) {
+  TableCache& C = cache();
+  std::lock_guard<std::mutex> g(C.mu);
+  auto key = std::make_tuple(F.id, log_count, limbs_key(base, F.limbs));
+  auto it = C.powers.find(key);
+  if (it != C.powers.end()) {
+    *out = static_cast<const uint32_t*>(it->second.p);
+    return GSN_OK;
+  }
+  if (!C.gen_stream) GSN_CUDA(cudaStreamCreateWithFlags(&C.gen_stream, cudaStreamNonBlocking));
+  const uint64_t count = (uint64_t)1 << log_count;
+  DevBuf b;
+  b.bytes = count * F.limbs * sizeof(uint32_t);
+  int rc = dev_alloc(&b.p, b.bytes);
+  if (rc) return rc;
+  cudaError_t e = F.powers(static_cast<uint32_t*>(b.p), count, base, C.gen_stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(C.gen_stream);
+  if (e != cudaSuccess) {
+    dev_free(b.p);
+    return cuda_fail(e, "twiddle generation");
+  }
+  count_launches(1);
+  C.powers[key] = b;
+  *out = static_cast<const uint32_t*>(b.p);
+  return GSN_OK;
+}
+
+// The default root table covering log_n: reuse any cached default table of
+// order >= 2^log_n (its powers include every smaller root's), else build one
+// of order 2^max(log_n, default_tw_log).
+static int default_twiddles(const FieldOps& F, int log_n, const uint32_t** tw, int* tw_log) {
+  {
+    TableCache& C = cache();
+    std::lock_guard<std::mutex> g(C.mu);
+    for (int k = log_n; k <= F.max_log_n; ++k) {
+      uint32_t r[kMaxLimbs];
+      F.root(k, r);
+      auto it = C.powers.find(std::make_tuple(F.id, k, limbs_key(r, F.limbs)));
+      if (it != C.powers.end()) {
+        *tw = static_cast<const uint32_t*>(it->second.p);
+        *tw_log = k;
+        return GSN_OK;
+      }
+    }
+  }
+  const int k = std::min(F.max_log_n, std::max(log_n, F.default_tw_log));
+  uint32_t r[kMaxLimbs];
+  F.root(k, r);
+  *tw_log = k;
+  return powers_table(F, r, k, tw);
+}
+
+int resolve_tables(const FieldOps& F, uint32_t log_n, const uint32_t* omega, int dir, const uint32_t* shift,
+                   Tables* T, cudaStream_t) {
+  if ((int)log_n > F.max_log_n || (int)log_n > F.two_adicity)
+    return set_error(GSN_ERR_SIZE, "log_n=%u exceeds the limit %d for field %d", log_n,
+                     std::min(F.max_log_n, F.two_adicity), F.id);
+  if (dir < GSN_FORWARD || dir > GSN_COSET_INVERSE) return set_error(GSN_ERR_ARG, "bad direction %d", dir);
+  const int N = F.limbs;
+  uint32_t def[kMaxLimbs];
+  F.root((int)log_n, def);
+  int rc;
+  if (!omega || std::memcmp(omega, def, sizeof(uint32_t) * N) == 0) {
+    rc = default_twiddles(F, (int)log_n, &T->tw, &T->tw_log);
+  } else {
+    if (!F.is_canonical(omega)) return set_error(GSN_ERR_OMEGA, "omega is not reduced below the modulus");
+    if (!F.is_primitive(omega, (int)log_n))
+      return set_error(GSN_ERR_OMEGA, "omega is not a primitive 2^%u-th root of unity", log_n);
+    T->tw_log = (int)log_n;
+    rc = powers_table(F, omega, (int)log_n, &T->tw);
+  }
+  if (rc) return rc;
+  T->inverse = (dir == GSN_INVERSE || dir == GSN_COSET_INVERSE) ? 1 : 0;
+  T->has_pre_const = 0;
+  T->pre_table = nullptr;
+  T->post_table = nullptr;
+  if (T->inverse) {
+    uint32_t nn[kMaxLimbs] = {0}, ninv[kMaxLimbs];
+    nn[0] = 1u << (log_n & 31);
+    if (log_n >= 32) {  // fields with more than one limb only (p32's limit is 28)
+      nn[0] = 0;
+      nn[log_n / 32] = 1u << (log_n % 32);
+    }
+    F.inv(nn, ninv);
+    F.to_mont(ninv, T->pre_const);
+    T->has_pre_const = 1;
+  }
+  if (dir == GSN_COSET_FORWARD || dir == GSN_COSET_INVERSE) {
+    uint32_t s[kMaxLimbs] = {0};
+    if (shift) {
+      if (!F.is_canonical(shift)) return set_error(GSN_ERR_ARG, "coset shift is not reduced below the modulus");
+      std::memcpy(s, shift, sizeof(uint32_t) * N);
+    } else {
+      s[0] = F.generator;
+    }
+    bool zero = true;
+    for (int i = 0; i < N; ++i) zero = zero && s[i] == 0;
+    if (zero) return set_error(GSN_ERR_ARG, "coset shift must be non-zero");
+    if (dir == GSN_COSET_FORWARD) {
+      rc = powers_table(F, s, (int)log_n, &T->pre_table);
+    } else {
+      uint32_t si[kMaxLimbs];
+      F.inv(s, si);
+      rc = powers_table(F, si, (int)log_n, &T->post_table);
+    }
+    if (rc) return rc;
+  }
+  return GSN_OK;
+}
+
+int scratch_for(cudaStream_t s, size_t bytes, uint32_t** out) {
+  TableCache& C = cache();
+  std::lock_guard<std::mutex> g(C.mu);
+  DevBuf& b = C.scratch[s];
+  if (b.bytes < bytes) {
+    if (b.p) {
+      GSN_CUDA(cudaStreamSynchronize(s));
+      dev_free(b.p);
+      b.p = nullptr;
+      b.bytes = 0;
+    }
+    int rc = dev_alloc(&b.p, bytes);
+    if (rc) return rc;
+    b.bytes = bytes;
+  }
+  *out = static_cast<uint32_t*>(b.p);
+  return GSN_OK;
+}
+
+int enqueue_ntt(const FieldOps& F, const Plan& plan, const Tables& T, uint32_t* data, uint32_t* scratch,
+                cudaStream_t s) {
+  PassArgs A;
+  std::memset(&A, 0, sizeof(A));
+  A.tw = T.tw;
+  A.tw_log = T.tw_log;
+  A.log_n = plan.log_n;
+  A.inverse = T.inverse;
+  A.npass = plan.npass;
+  for (int i = 0; i < kMaxPasses; ++i) A.radix_log[i] = plan.radix_log[i];
+  int outer = 0;
+  for (int p = 0; p < plan.npass; ++p) {
+    A.first = p == 0;
+    A.last = p == plan.npass - 1;
+    A.src = A.first ? data : scratch;
+    A.dst = A.last ? data : scratch;
+    A.log_r = plan.radix_log[p];
+    A.log_outer = outer;
+    A.log_inner = plan.log_n - outer - plan.radix_log[p];
+    A.log_j = plan.log_j[p];
+    A.tiles = (uint64_t)1 << (plan.log_n - A.log_r - A.log_j);
+    A.pre_table = A.first ? T.pre_table : nullptr;
+    A.post_table = A.last ? T.post_table : nullptr;
+    A.has_pre_const = A.first ? T.has_pre_const : 0;
+    if (A.has_pre_const) std::memcpy(A.pre_const, T.pre_const, sizeof(A.pre_const));
+    cudaError_t e = F.pass(A, plan.block[p], s);
+    if (e != cudaSuccess) return cuda_fail(e, "NTT pass launch");
+    count_launches(1);
+    outer += plan.radix_log[p];
+  }
+  return GSN_OK;
+}
+
+static int check_data_ptr(const FieldOps& F, const void* p) {
+  if (!p) return set_error(GSN_ERR_ARG, "null data pointer");
+  const uintptr_t align = (F.limbs % 4 == 0) ? 16 : 4;
+  if (reinterpret_cast<uintptr_t>(p) % align)
+    return set_error(GSN_ERR_ARG, "data pointer must be %zu-byte aligned", (size_t)align);
+  return GSN_OK;
+}
+
+static int ntt_impl(int field, uint32_t* data, uint32_t log_n, const uint32_t* omega, int dir,
+                    const uint32_t* shift, uint32_t* scratch, cudaStream_t s) {
+  const FieldOps* F = field_ops(field);
+  if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);
+  int rc = check_data_ptr(*F, data);
+  if (rc) return rc;
+  Tables T;
+  rc = resolve_tables(*F, log_n, omega, dir, shift, &T, s);
+  if (rc) return rc;
+  Plan plan = plan_for(*F, (int)log_n);
+  if (plan.npass > 1 && !scratch) {
+    rc = scratch_for(s, ((size_t)1 << log_n) * F->limbs * sizeof(uint32_t), &scratch);
+    if (rc) return rc;
+  }
+  return enqueue_ntt(*F, plan, T, data, scratch, s);
+}
+
+static std::mutex g_host_mu;
+
+}  // namespace gsn
+
+using namespace gsn;
+
+extern "C" {
+
+const char* gsn_last_error(void) { return t_error.c_str(); }
+
+int gsn_version(void) { return 100; }
+
+int gsn_field_limbs(int field) {
+  const FieldOps* F = field_ops(field);
+  return F ? F->limbs : -GSN_ERR_FIELD;
+}
+
+int gsn_field_two_adicity(int field) {
+  const FieldOps* F = field_ops(field);
+  return F ? F->two_adicity : -GSN_ERR_FIELD;
+}
+
+int gsn_field_max_log_n(int field) {
+  const FieldOps* F = field_ops(field);
+  return F ? std::min(F->max_log_n, F->two_adicity) : -GSN_ERR_FIELD;
+}
+
+int gsn_field_modulus(int field, uint32_t* out) {
+  const FieldOps* F = field_ops(field);
+  if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);
+  if (!out) return set_error(GSN_ERR_ARG, "null output");
+  F->modulus(out);
+  return GSN_OK;
+}
+
+int gsn_root_of_unity(int field, uint32_t log_n, uint32_t* out) {
+  const FieldOps* F = field_ops(field);
+  if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);
+  if (!out) return set_error(GSN_ERR_ARG, "null output");
+  if ((int)log_n > F->two_adicity) return set_error(GSN_ERR_SIZE, "log_n exceeds the 2-adicity");
+  F->root((int)log_n, out);
+  return GSN_OK;
+}
+
+int gsn_ntt(int field, uint32_t* data, uint32_t log_n, const uint32_t* omega, int dir, const uint32_t* shift,
+            void* stream) {
+  return ntt_impl(field, data, log_n, omega, dir, shift, nullptr, static_cast<cudaStream_t>(stream));
+}
+
+int gsn_ntt_scratch(int field, uint32_t* data, uint32_t log_n, const uint32_t* omega, int dir,
+                    const uint32_t* shift, uint32_t* scratch, void* stream) {
+  if (!scratch) return set_error(GSN_ERR_ARG, "null scratch");
+  return ntt_impl(field, data, log_n, omega, dir, shift, scratch, static_cast<cudaStream_t>(stream));
+}
+
+int gsn_ntt_host(int field, uint32_t* data, uint32_t log_n, const uint32_t* omega, int dir,
+                 const uint32_t* shift) {
+  const FieldOps* F = field_ops(field);
+  if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);
+  if (!data) return set_error(GSN_ERR_ARG, "null data pointer");
+  if ((int)log_n > std::min(F->max_log_n, F->two_adicity))
+    return set_error(GSN_ERR_SIZE, "log_n=%u exceeds the limit for field %d", log_n, field);
+  std::lock_guard<std::mutex> g(g_host_mu);
+  static cudaStream_t stream = nullptr;
+  static DevBuf buf;
+  if (!stream) GSN_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  const size_t bytes = ((size_t)1 << log_n) * F->limbs * sizeof(uint32_t);
+  if (buf.bytes < bytes) {
+    dev_free(buf.p);
+    buf.p = nullptr;
+    buf.bytes = 0;
+    int rc = dev_alloc(&buf.p, bytes);
+    if (rc) return rc;
+    buf.bytes = bytes;
+  }
+  uint32_t* dev = static_cast<uint32_t*>(buf.p);
+  GSN_CUDA(cudaMemcpyAsync(dev, data, bytes, cudaMemcpyHostToDevice, stream));
+  int rc = ntt_impl(field, dev, log_n, omega, dir, shift, nullptr, stream);
+  if (rc) {
+    cudaStreamSynchronize(stream);
+    return rc;
+  }
+  GSN_CUDA(cudaMemcpyAsync(data, dev, bytes, cudaMemcpyDeviceToHost, stream));
+  GSN_CUDA(cudaStreamSynchronize(stream));
+  return GSN_OK;
+}
+
+int gsn_prepare(int field, uint32_t log_n, const uint32_t* omega) {
+  const FieldOps* F = field_ops(field);
+  if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);
+  Tables T;
+  return resolve_tables(*F, log_n, omega, GSN_FORWARD, nullptr, &T, nullptr);
+}
+
+int gsn_pointwise_mul(int field, uint32_t* a, const uint32_t* b, uint64_t n, void* stream) {
+  const FieldOps* F = field_ops(field);
+  if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);
+  int rc = check_data_ptr(*F, a);
+  if (rc) return rc;
+  rc = check_data_ptr(*F, b);
+  if (rc) return rc;
+  if (n == 0) return GSN_OK;
+  cudaError_t e = F->pointwise(a, b, n, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "pointwise multiply launch");
+  count_launches(1);
+  return GSN_OK;
+}
+
+int gsn_synchronize(void* stream) {
+  GSN_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
+  return GSN_OK;
+}
+
+int gsn_host_alloc(void** ptr, size_t bytes) {
+  if (!ptr) return set_error(GSN_ERR_ARG, "null output");
+  cudaError_t e = cudaMallocHost(ptr, bytes ? bytes : 16);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(GSN_ERR_NOMEM, "cudaMallocHost(%zu) failed: %s", bytes, cudaGetErrorString(e));
+  }
+  return GSN_OK;
+}
+
+int gsn_host_free(void* ptr) {
+  if (ptr) GSN_CUDA(cudaFreeHost(ptr));
+  return GSN_OK;
+}
+
+int gsn_release_caches(void) {
+  TableCache& C = cache();
+  std::lock_guard<std::mutex> g(C.mu);
+  GSN_CUDA(cudaDeviceSynchronize());
+  for (auto& kv : C.powers) dev_free(kv.second.p);
+  C.powers.clear();
+  for (auto& kv : C.scratch) dev_free(kv.second.p);
+  C.scratch.clear();
+  return GSN_OK;
+}
+
+uint64_t gsn_kernel_launch_count(void) { return g_launches.load(); }
+
+}  // extern "C"

@@ -1,0 +1,74 @@
+// Internal runtime shared by the C ABI, the batch planner and the server.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "field_ops.h"
+#include "ntt_common.h"
+
+namespace gsn {
+
+int set_error(int code, const char* fmt, ...);
+int cuda_fail(cudaError_t e, const char* what);
+
+#define GSN_CUDA(call)                                        \
+  do {                                                        \
+    cudaError_t gsn_e_ = (call);                              \
+    if (gsn_e_ != cudaSuccess) return cuda_fail(gsn_e_, #call); \
+  } while (0)
+
+void count_launches(uint64_t n);
+
+// A transform plan: pass split, tile shape and threads per pass.
+struct Plan {
+  int log_n = 0;
+  int npass = 0;
+  int radix_log[kMaxPasses] = {0, 0, 0, 0};
+  int log_j[kMaxPasses] = {0, 0, 0, 0};
+  int block[kMaxPasses] = {0, 0, 0, 0};
+};
+
+// Default plan for (field, log_n), or the tuned one when a tuning table is
+// loaded.
+Plan plan_for(const FieldOps& F, int log_n);
+// Heuristic plan with explicit limits (used by the autotuner's candidate set).
+Plan make_plan(const FieldOps& F, int log_n, int max_r, int target_j, int max_block);
+bool plan_valid(const FieldOps& F, const Plan& p);
+size_t plan_smem_bytes(const FieldOps& F, const Plan& p, int pass);
+void set_tuned_plan(int field, int log_n, const Plan& p);
+void clear_tuned_plans();
+bool get_tuned_plan(int field, int log_n, Plan* out);
+
+// Resolved twiddle / coset tables for one transform.
+struct Tables {
+  const uint32_t* tw = nullptr;
+  int tw_log = 0;
+  const uint32_t* pre_table = nullptr;
+  const uint32_t* post_table = nullptr;
+  int has_pre_const = 0;
+  uint32_t pre_const[kMaxLimbs] = {0};
+  int inverse = 0;
+};
+
+// Validates arguments and resolves (and caches) all tables for a transform.
+int resolve_tables(const FieldOps& F, uint32_t log_n, const uint32_t* omega, int dir, const uint32_t* shift,
+                   Tables* out, cudaStream_t s);
+
+// Enqueues the passes of one transform.
+int enqueue_ntt(const FieldOps& F, const Plan& plan, const Tables& T, uint32_t* data, uint32_t* scratch,
+                cudaStream_t s);
+
+// Library-owned per-stream scratch (grow-only).
+int scratch_for(cudaStream_t s, size_t bytes, uint32_t** out);
+
+// Device allocation bookkeeping (for tests / stats).
+int dev_alloc(void** p, size_t bytes);
+void dev_free(void* p);
+
+}  // namespace gsn

@@ -33,6 +33,8 @@ def render() -> str:
         "#pragma once",
         "#include <cstdint>",
         "",
+        "#include \"gsn_compat.h\"",
+        "",
         "namespace gsn {",
         "",
     ]

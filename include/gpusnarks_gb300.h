@@ -1,0 +1,117 @@
+/*
+ * gpusnarks_gb300: GB300-native finite-field NTT, C ABI.
+ *
+ * This is the drop-in boundary for the reference's FFT path.  Every entry
+ * point returns GSN_OK (0) or a GSN_ERR_* code and never exits or asserts;
+ * gsn_last_error() gives the message of the last failure on the calling
+ * thread.  No function takes or returns a torch or C++ type.
+ *
+ * Element layout (all fields): an element is LIMBS little-endian uint32
+ * words, exactly the reference's `uint32_t im_rep[SIZE]`
+ * (cuda/device_field.h:75); an array of n elements is n*LIMBS words,
+ * element-major.  Transforms are representation-agnostic (linear): the output
+ * is in whatever representation the input was stored in (canonical or
+ * Montgomery), reduced to [0, p).  `omega` and `shift` arguments are
+ * canonical integers.
+ *
+ * Reference interfaces replaced:
+ *   best_fft<FieldT>(std::vector<FieldT>&, const FieldT& omg)
+ *       cuda/fft_kernel.h:24-25, cuda/fft_kernel.cu:144-174
+ *       -> gsn_ntt_host (and the C++ shim include/gsn_best_fft.h)
+ *   the device launch inside it (cuda_fft<<<blocks,threads>>>, :162)
+ *       -> gsn_ntt on caller-owned device memory
+ *   the omega powers computed per thread by Scalar::pow
+ *       (cuda/device_field_operators.h:229-257, fft_kernel.cu:92-95)
+ *       -> gsn_prepare (device-resident twiddle tables)
+ */
+#ifndef GPUSNARKS_GB300_H
+#define GPUSNARKS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Fields.  GSN_MNT4753_FR is the MNT4-753 scalar field r
+ * (cuda/device_field.h:445-446); the reference compiles in the base field q
+ * (device_field.h:62-65), whose 2-adicity (15) admits no 2^16-point NTT. */
+typedef enum gsn_field {
+  GSN_P32 = 0,          /* 3*2^30 + 1, 1 limb, generator 5      */
+  GSN_BLS12_381_FR = 1, /* BLS12-381 r, 8 limbs, generator 7    */
+  GSN_MNT4753_FR = 2    /* MNT4-753 r, 24 limbs, generator 11   */
+} gsn_field;
+
+typedef enum gsn_dir {
+  GSN_FORWARD = 0,       /* X[k] = sum_j x[j] w^(jk)                    */
+  GSN_INVERSE = 1,       /* x[j] = n^-1 sum_k X[k] w^(-jk)              */
+  GSN_COSET_FORWARD = 2, /* X[k] = sum_j x[j] s^j w^(jk)                */
+  GSN_COSET_INVERSE = 3  /* inverse of GSN_COSET_FORWARD                */
+} gsn_dir;
+
+enum {
+  GSN_OK = 0,
+  GSN_ERR_ARG = 1,     /* bad pointer, alignment or enum value         */
+  GSN_ERR_FIELD = 2,   /* unknown field id                             */
+  GSN_ERR_SIZE = 3,    /* log_n outside [0, min(2-adicity, limit)]     */
+  GSN_ERR_OMEGA = 4,   /* omega is not a primitive 2^log_n-th root     */
+  GSN_ERR_CUDA = 5,    /* a CUDA runtime call failed                   */
+  GSN_ERR_NOMEM = 6,   /* device or host allocation failed / budget    */
+  GSN_ERR_BUSY = 7,    /* resource in use (server full, ...)           */
+  GSN_ERR_TIMEOUT = 8, /* a bounded device wait gave up                */
+  GSN_ERR_STATE = 9    /* call not valid in the object's current state */
+};
+
+/* ---- library / field information --------------------------------------- */
+const char* gsn_last_error(void);
+int gsn_version(void);
+int gsn_field_limbs(int field);
+int gsn_field_two_adicity(int field);
+int gsn_field_max_log_n(int field);
+int gsn_field_modulus(int field, uint32_t* out_limbs);
+/* canonical g^((p-1)/2^log_n): the default forward root for size 2^log_n */
+int gsn_root_of_unity(int field, uint32_t log_n, uint32_t* out_limbs);
+
+/* ---- single transforms --------------------------------------------------- */
+
+/* In-place transform of n = 2^log_n elements in device memory.
+ * omega: NULL for gsn_root_of_unity(field, log_n), else the canonical forward
+ *        root (inverse directions use its inverse).
+ * shift: coset shift for the coset directions, canonical; NULL = generator.
+ * stream: a cudaStream_t (NULL = the default stream).  Asynchronous. */
+int gsn_ntt(int field, uint32_t* data, uint32_t log_n, const uint32_t* omega, int dir,
+            const uint32_t* shift, void* stream);
+
+/* Same, using caller-provided scratch of at least n elements (device) instead
+ * of the library's per-stream scratch. */
+int gsn_ntt_scratch(int field, uint32_t* data, uint32_t log_n, const uint32_t* omega, int dir,
+                    const uint32_t* shift, uint32_t* scratch, void* stream);
+
+/* best_fft drop-in: `data` is host memory (pageable or pinned), transformed
+ * in place; host->device copy, transform, device->host copy; returns when the
+ * result is back in `data`.  Unlike cuda/fft_kernel.cu:144-174 it honours
+ * omega, accepts any power-of-two size up to the field limit, frees what it
+ * allocates and reports errors instead of exiting. */
+int gsn_ntt_host(int field, uint32_t* data, uint32_t log_n, const uint32_t* omega, int dir,
+                 const uint32_t* shift);
+
+/* Build and cache the twiddle table for (field, log_n, omega). */
+int gsn_prepare(int field, uint32_t log_n, const uint32_t* omega);
+
+/* a[i] = a[i] * b[i] mod p on device memory (canonical values). */
+int gsn_pointwise_mul(int field, uint32_t* a, const uint32_t* b, uint64_t n, void* stream);
+
+/* ---- memory helpers ------------------------------------------------------ */
+int gsn_synchronize(void* stream);
+int gsn_host_alloc(void** ptr, size_t bytes);  /* pinned host memory */
+int gsn_host_free(void* ptr);
+int gsn_release_caches(void);                  /* free twiddle tables and scratch */
+/* number of NTT-path kernel launches issued by this library so far */
+uint64_t gsn_kernel_launch_count(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPUSNARKS_GB300_H */

