@@ -48,7 +48,26 @@ _SIGNATURES = [
     ("gsn_host_free", ctypes.c_int, [ctypes.c_void_p]),
     ("gsn_release_caches", ctypes.c_int, []),
     ("gsn_kernel_launch_count", ctypes.c_uint64, []),
+    ("gsn_microbench_imad", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
+                                           ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    ("gsn_batch_create", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
+                                        ctypes.POINTER(ctypes.c_void_p)]),
+    ("gsn_batch_launch", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    ("gsn_batch_launch_per_call", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
+    ("gsn_batch_status", ctypes.c_int, [ctypes.c_void_p]),
+    ("gsn_batch_info", ctypes.c_int, [ctypes.c_void_p, ctypes.POINTER(ctypes.c_uint64),
+                                      ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
+                                      ctypes.POINTER(ctypes.c_uint64)]),
+    ("gsn_batch_destroy", ctypes.c_int, [ctypes.c_void_p]),
+    ("gsn_fill_random", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
+                                       ctypes.c_void_p]),
 ]
+
+
+class BatchJob(ctypes.Structure):
+    """Mirror of gsn_batch_job (include/gpusnarks_gb300.h)."""
+    _fields_ = [("data", ctypes.c_void_p), ("log_n", ctypes.c_uint32), ("dir", ctypes.c_int32),
+                ("omega", ctypes.c_void_p), ("shift", ctypes.c_void_p)]
 
 
 def library_path() -> pathlib.Path:

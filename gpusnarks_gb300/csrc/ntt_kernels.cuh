@@ -206,6 +206,50 @@ __global__ void gen_powers_kernel(uint32_t* out, uint64_t count, Fe<P> base) {
   }
 }
 
+// Uniform elements of [0, p): limb j of attempt a of element i is the low
+// word of splitmix64's finaliser applied to
+//   seed + (i * 64 * N + a * N + j + 1) * 0x9E3779B97F4A7C15,
+// the top limb is masked to bitlen(p) and attempts repeat until the value is
+// below p (64 attempts at most; the acceptance rate is at least 1/2).
+__device__ __forceinline__ uint64_t splitmix_mix(uint64_t z) {
+  z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+  z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+  return z ^ (z >> 31);
+}
+
+template <class P>
+__global__ void fill_random_kernel(uint32_t* out, uint64_t n, uint64_t seed) {
+  constexpr int N = P::N;
+  constexpr int top_bits = P::BITS - 32 * (N - 1);
+  constexpr uint32_t top_mask = top_bits >= 32 ? 0xFFFFFFFFu : ((1u << top_bits) - 1u);
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    Fe<P> x;
+    bool ok = false;
+    for (int a = 0; a < 64 && !ok; ++a) {
+#pragma unroll
+      for (int j = 0; j < N; ++j) {
+        const uint64_t ctr = i * 64ull * N + (uint64_t)a * N + j + 1;
+        x.l[j] = (uint32_t)splitmix_mix(seed + ctr * 0x9E3779B97F4A7C15ull);
+      }
+      x.l[N - 1] &= top_mask;
+      bool lt = false, decided = false;
+#pragma unroll
+      for (int j = N - 1; j >= 0; --j) {
+        if (!decided && x.l[j] != P::mod(j)) {
+          lt = x.l[j] < P::mod(j);
+          decided = true;
+        }
+      }
+      ok = lt;
+    }
+    if (!ok)
+#pragma unroll
+      for (int j = 0; j < N; ++j) x.l[j] = 0;
+    fe_store<P>(out + i * N, x);
+  }
+}
+
 // a[i] = a[i] * b[i] mod p (canonical in, canonical out): two Montgomery
 // products, the second by R^2.
 template <class P>
@@ -348,6 +392,14 @@ struct Kernels {
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, block, smem) != cudaSuccess) return 0;
     return nb;
+  }
+  static cudaError_t fill(uint32_t* out, uint64_t n, uint64_t seed, cudaStream_t s) {
+    const int block = 256;
+    uint64_t grid = (n + block - 1) / block;
+    if (grid > 152 * 64) grid = 152 * 64;
+    if (grid == 0) return cudaSuccess;
+    fill_random_kernel<P><<<(unsigned)grid, block, 0, s>>>(out, n, seed);
+    return cudaGetLastError();
   }
   static cudaError_t pointwise(uint32_t* a, const uint32_t* b, uint64_t n, cudaStream_t s) {
     const int block = 256;

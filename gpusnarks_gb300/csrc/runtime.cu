@@ -185,6 +185,22 @@ static std::string limbs_key(const uint32_t* x, int n) {
   return std::string(reinterpret_cast<const char*>(x), sizeof(uint32_t) * n);
 }
 
+// g^((p-1)/2^log_n), memoised: the exponentiation costs up to ~1 ms on the
+// host for the 753-bit field and every call needs it.
+static void default_root(const FieldOps& F, int log_n, uint32_t* out) {
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, std::string> memo;
+  std::lock_guard<std::mutex> g(mu);
+  auto key = std::make_pair(F.id, log_n);
+  auto it = memo.find(key);
+  if (it == memo.end()) {
+    uint32_t r[kMaxLimbs];
+    F.root(log_n, r);
+    it = memo.emplace(key, limbs_key(r, F.limbs)).first;
+  }
+  std::memcpy(out, it->second.data(), it->second.size());
+}
+
 // Returns a cached table of base^e * R for e in [0, 2^log_count); builds it
 // on first use.  Caller holds no lock.
 static int powers_table(const FieldOps& F, const uint32_t* base, int log_count, const uint32_t** out) {
@@ -223,7 +239,7 @@ static int default_twiddles(const FieldOps& F, int log_n, const uint32_t** tw, i
     std::lock_guard<std::mutex> g(C.mu);
     for (int k = log_n; k <= F.max_log_n; ++k) {
       uint32_t r[kMaxLimbs];
-      F.root(k, r);
+      default_root(F, k, r);
       auto it = C.powers.find(std::make_tuple(F.id, k, limbs_key(r, F.limbs)));
       if (it != C.powers.end()) {
         *tw = static_cast<const uint32_t*>(it->second.p);
@@ -234,7 +250,7 @@ static int default_twiddles(const FieldOps& F, int log_n, const uint32_t** tw, i
   }
   const int k = std::min(F.max_log_n, std::max(log_n, F.default_tw_log));
   uint32_t r[kMaxLimbs];
-  F.root(k, r);
+  default_root(F, k, r);
   *tw_log = k;
   return powers_table(F, r, k, tw);
 }
@@ -247,7 +263,7 @@ int resolve_tables(const FieldOps& F, uint32_t log_n, const uint32_t* omega, int
   if (dir < GSN_FORWARD || dir > GSN_COSET_INVERSE) return set_error(GSN_ERR_ARG, "bad direction %d", dir);
   const int N = F.limbs;
   uint32_t def[kMaxLimbs];
-  F.root((int)log_n, def);
+  default_root(F, (int)log_n, def);
   int rc;
   if (!omega || std::memcmp(omega, def, sizeof(uint32_t) * N) == 0) {
     rc = default_twiddles(F, (int)log_n, &T->tw, &T->tw_log);

@@ -129,6 +129,42 @@ class Field:
         return out.reshape(self.shape(n))
 
 
+    def device_random(self, n: int, seed: int, start: int = 0) -> np.ndarray:
+        """Host replica of gsn_fill_random: elements [start, start+n) of the stream.
+
+        Limb j of attempt a of element i is the low word of splitmix64's
+        finaliser of seed + (i*64*N + a*N + j + 1) * 0x9E3779B97F4A7C15; the
+        top limb is masked to bitlen(p) and the first attempt below p wins.
+        """
+        N = self.limbs
+        top_bits = self.p.bit_length() - 32 * (N - 1)
+        top_mask = np.uint64((1 << top_bits) - 1) if top_bits < 32 else np.uint64(0xFFFFFFFF)
+        p_limbs = self.to_limbs(self.p)
+        idx = np.arange(start, start + n, dtype=np.uint64)
+        out = np.zeros((n, N), dtype=np.uint32)
+        done = np.zeros(n, dtype=bool)
+        golden = np.uint64(0x9E3779B97F4A7C15)
+        with np.errstate(over="ignore"):
+            for a in range(64):
+                if done.all():
+                    break
+                cand = np.empty((n, N), dtype=np.uint32)
+                for j in range(N):
+                    ctr = idx * np.uint64(64 * N) + np.uint64(a * N + j + 1)
+                    z = np.uint64(seed) + ctr * golden
+                    z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+                    z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+                    z = z ^ (z >> np.uint64(31))
+                    w = z & np.uint64(0xFFFFFFFF)
+                    if j == N - 1:
+                        w &= top_mask
+                    cand[:, j] = w.astype(np.uint32)
+                ok = _lt_limbs(cand, p_limbs) & ~done
+                out[ok] = cand[ok]
+                done |= ok
+        return out.reshape(self.shape(n))
+
+
 def _splitmix_words(state: np.uint64, count: int):
     """``count`` 32-bit words from a splitmix64 stream (two per output)."""
     m = (count + 1) // 2

@@ -102,6 +102,42 @@ int gsn_prepare(int field, uint32_t log_n, const uint32_t* omega);
 /* a[i] = a[i] * b[i] mod p on device memory (canonical values). */
 int gsn_pointwise_mul(int field, uint32_t* a, const uint32_t* b, uint64_t n, void* stream);
 
+/* ---- batched transforms (no reference counterpart: the reference runs one
+ * transform per best_fft call) --------------------------------------------- */
+
+typedef struct gsn_batch gsn_batch; /* opaque */
+
+typedef struct gsn_batch_job {
+  uint32_t* data;        /* device memory, 2^log_n elements, transformed in place */
+  uint32_t log_n;
+  int32_t dir;           /* gsn_dir */
+  const uint32_t* omega; /* canonical forward root, NULL = default */
+  const uint32_t* shift; /* coset shift, NULL = field generator */
+} gsn_batch_job;
+
+enum { GSN_BATCH_GRAPH = 1 }; /* capture the launch into a CUDA graph */
+
+/* Plans every job (radix/tile per log_n from the tuning table), builds the
+ * device work queue, allocates per-job scratch and resolves twiddle tables.
+ * All jobs share one field.  With GSN_BATCH_GRAPH the launch is captured
+ * into a CUDA graph once and replayed by gsn_batch_launch. */
+int gsn_batch_create(int field, const gsn_batch_job* jobs, size_t njobs, int flags, gsn_batch** out);
+/* All jobs in one persistent launch (asynchronous on `stream`). */
+int gsn_batch_launch(gsn_batch* b, void* stream);
+/* The same jobs issued one gsn_ntt call at a time (the per-call baseline). */
+int gsn_batch_launch_per_call(gsn_batch* b, void* stream);
+/* After the stream has drained: GSN_OK, or GSN_ERR_TIMEOUT if a bounded
+ * device wait of the last gsn_batch_launch gave up. */
+int gsn_batch_status(gsn_batch* b);
+/* njobs, work items (tiles), total elements, device bytes held */
+int gsn_batch_info(gsn_batch* b, uint64_t* njobs, uint64_t* nwork, uint64_t* elements, uint64_t* device_bytes);
+int gsn_batch_destroy(gsn_batch* b);
+
+/* Fill device memory with uniform elements of [0, p): element i, limb j are
+ * drawn from splitmix64 of (seed, i, attempt) with rejection sampling;
+ * deterministic for a given seed. */
+int gsn_fill_random(int field, uint32_t* data, uint64_t n, uint64_t seed, void* stream);
+
 /* ---- memory helpers ------------------------------------------------------ */
 int gsn_synchronize(void* stream);
 int gsn_host_alloc(void** ptr, size_t bytes);  /* pinned host memory */
@@ -109,6 +145,13 @@ int gsn_host_free(void* ptr);
 int gsn_release_caches(void);                  /* free twiddle tables and scratch */
 /* number of NTT-path kernel launches issued by this library so far */
 uint64_t gsn_kernel_launch_count(void);
+
+/* ---- measurement --------------------------------------------------------- */
+/* Integer-pipe roofline denominator (no reference counterpart): throughput of
+ * the PTX carry-chain multiply-adds (mad.lo.cc / madc.hi.cc) the big-field
+ * Montgomery products use, on every SM at full occupancy.  Returns PTX
+ * multiply-adds per second, per SM per clock, and the SM clock seen. */
+int gsn_microbench_imad(int iters, double* mads_per_s, double* mads_per_clk_sm, double* sm_mhz);
 
 #ifdef __cplusplus
 }
