@@ -99,7 +99,7 @@ int gsn_batch_create(int field, const gsn_batch_job* jobs, size_t njobs, int fla
       batch_free(b);
       return rc;
     }
-    Plan p = plan_for(*F, (int)u.log_n);
+    Plan p = plan_for(*F, (int)u.log_n, /*batched=*/true);
     b->plans[i] = p;
     BatchJob& J = b->jobs[i];
     std::memset(&J, 0, sizeof(J));

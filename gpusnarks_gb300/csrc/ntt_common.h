@@ -69,6 +69,24 @@ struct BatchJob {
   uint32_t pre_const[kMaxLimbs];
 };
 
+// Arguments of the register-blocked 32-bit pass (ntt_p32.cuh).  Tables are
+// built for the root actually used (omega^-1 for inverse transforms).
+struct P32Args {
+  const uint32_t* src;
+  uint32_t* dst;
+  const uint32_t* tw_tile;     // omega_R^e * R, e < 2^(log_r - 1)
+  const uint32_t* tw_lo;       // omega_n^e * R, e < 2^lo_bits
+  const uint32_t* tw_hi;       // omega_n^(e << lo_bits) * R
+  const uint32_t* pre_table;   // first pass: x[i] *= pre_table[i]
+  const uint32_t* post_table;  // last pass: X[k] *= post_table[k]
+  uint64_t tiles;
+  uint32_t pre_const;          // first pass: x *= pre_const (Montgomery form)
+  int has_pre_const;
+  int lo_bits;
+  int log_n, log_r, log_inner, log_outer, log_j, last, first, npass;
+  int radix_log[kMaxPasses];
+};
+
 __host__ __device__ inline uint64_t pass_tiles(int log_n, int npass, const int* radix_log, int p, int log_j) {
   (void)npass;
   (void)radix_log;

@@ -1,7 +1,13 @@
 // Kernels and host helpers for the 32-bit field p = 3*2^30 + 1.
 #include "field_impl.cuh"
+#include "ntt_p32.cuh"
+#include "runtime.h"
 
 namespace gsn {
 // 2^28 elements (1 GiB) is the largest size exercised; the 2-adicity is 30.
 const FieldOps kOpsP32 = make_field_ops<FieldP32>(28, 16);
+
+cudaError_t launch_p32_pass(const P32Args& A, int e_log, int block, int grid_cap, cudaStream_t s) {
+  return P32Kernels::launch(A, e_log, block, grid_cap, s);
+}
 }  // namespace gsn

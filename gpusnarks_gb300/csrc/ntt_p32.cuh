@@ -1,0 +1,271 @@
+// Register-blocked NTT pass for the 32-bit field p = 3*2^30 + 1.
+//
+// Same four-step pass decomposition and tile geometry as ntt_tile
+// (ntt_common.h), but the tile's radix-2^r DIF runs in register sub-steps:
+// each thread holds E = 2^ET rows x 4 adjacent columns (one uint4 per row)
+// and performs ET butterfly stages on them between two shared-memory round
+// trips, so a 2^12-point tile costs three exchanges instead of twelve.
+// Global traffic is 16-byte vectors; the last pass (contiguous input rows)
+// transposes 4x4 blocks in registers so shared-memory stores stay 16-byte.
+//
+// Shared-memory layout: the tile is 2^r rows of J = 4*CG words; the 16-byte
+// chunk (row, cg) is stored at chunk index ((row*CG + cg) XOR (CG * f(row)))
+// where f(row) XOR-folds the row bits above the ones that select a chunk
+// inside a 128-byte bank line.  That map is a bijection and keeps every
+// access pattern of this kernel (row-major loads, transposed loads, radix-E
+// sub-steps at every stride, bit-reversed stores) free of bank conflicts.
+//
+// Twiddles: in-tile stages read a compact table of omega_R^e (e < R/2) for the
+// pass radix R; the four-step twiddle omega_n^e is LO[e mod 2^lo] * HI[e >> lo]
+// from two small tables.  All tables hold Montgomery forms (x * 2^32 mod p),
+// built for the root actually used (omega^-1 for inverse transforms).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "arith.cuh"
+#include "ntt_common.h"
+#include "ntt_kernels.cuh"
+
+namespace gsn {
+
+// P32Args is declared in ntt_common.h.
+
+namespace p32 {
+
+using F = FieldP32;
+
+template <int LCG>
+__device__ __forceinline__ uint32_t chunk_of(uint32_t row, uint32_t cg) {
+  constexpr int SH = 3 - LCG;  // row bits that pick a chunk inside a 128-byte line
+  uint32_t x = row >> SH;
+  if constexpr (SH == 1) {
+    x ^= x >> 8;
+    x ^= x >> 4;
+    x ^= x >> 2;
+    x ^= x >> 1;
+  } else if constexpr (SH == 2) {
+    x ^= x >> 8;
+    x ^= x >> 4;
+    x ^= x >> 2;
+  } else {
+    x ^= x >> 9;
+    x ^= x >> 6;
+    x ^= x >> 3;
+  }
+  const uint32_t f = x & ((1u << SH) - 1u);
+  return ((row << LCG) | cg) ^ (f << LCG);
+}
+
+template <int LCG>
+__device__ __forceinline__ uint4 sm_ld(const uint4* sm, uint32_t row, uint32_t cg) {
+  return sm[chunk_of<LCG>(row, cg)];
+}
+template <int LCG>
+__device__ __forceinline__ void sm_st(uint4* sm, uint32_t row, uint32_t cg, uint4 v) {
+  sm[chunk_of<LCG>(row, cg)] = v;
+}
+
+__device__ __forceinline__ uint32_t mm(uint32_t a, uint32_t b) { return mul1<F>(a, b); }
+
+__device__ __forceinline__ uint4 mul4(uint4 a, uint32_t w) {
+  return make_uint4(mm(a.x, w), mm(a.y, w), mm(a.z, w), mm(a.w, w));
+}
+__device__ __forceinline__ uint4 mul4v(uint4 a, uint4 w) {
+  return make_uint4(mm(a.x, w.x), mm(a.y, w.y), mm(a.z, w.z), mm(a.w, w.w));
+}
+
+// DIF butterfly on 4 columns: (a, b) -> (a + b, (a - b) * w)
+__device__ __forceinline__ void bfly4(uint4& a, uint4& b, uint32_t w) {
+  uint4 s, d;
+  s.x = add1<F>(a.x, b.x);
+  d.x = sub1<F>(a.x, b.x);
+  s.y = add1<F>(a.y, b.y);
+  d.y = sub1<F>(a.y, b.y);
+  s.z = add1<F>(a.z, b.z);
+  d.z = sub1<F>(a.z, b.z);
+  s.w = add1<F>(a.w, b.w);
+  d.w = sub1<F>(a.w, b.w);
+  a = s;
+  b = mul4(d, w);
+}
+
+__device__ __forceinline__ uint32_t tw_n(const P32Args& A, uint64_t e) {
+  const uint32_t lo = __ldg(A.tw_lo + (e & ((1ull << A.lo_bits) - 1)));
+  const uint32_t hi = __ldg(A.tw_hi + (e >> A.lo_bits));
+  return mm(lo, hi);
+}
+
+__device__ __forceinline__ uint4 premul(const P32Args& A, uint4 x, uint64_t g) {
+  if (A.pre_table) x = mul4v(x, __ldg(reinterpret_cast<const uint4*>(A.pre_table + g)));
+  if (A.has_pre_const) x = mul4(x, A.pre_const);
+  return x;
+}
+
+// One register sub-step: rows rowbase + m * 2^ls (m < 2^ET), stages s0..s0+ET-1.
+template <int ET, int LCG>
+__device__ __forceinline__ void substep(uint4* sm, const uint32_t* __restrict__ twt, uint32_t rowbase, uint32_t cg,
+                                        int ls, int s0, uint32_t low) {
+  constexpr int E = 1 << ET;
+  uint4 x[E];
+#pragma unroll
+  for (int m = 0; m < E; ++m) x[m] = sm_ld<LCG>(sm, rowbase + ((uint32_t)m << ls), cg);
+#pragma unroll
+  for (int q = 0; q < ET; ++q) {
+#pragma unroll
+    for (int t = 0; t < (E >> (q + 1)); ++t) {
+      const uint32_t w = __ldg(twt + ((((uint32_t)t << ls) + low) << (s0 + q)));
+#pragma unroll
+      for (int g = 0; g < (1 << q); ++g) {
+        const int m = g * (E >> q) + t;
+        bfly4(x[m], x[m + (E >> (q + 1))], w);
+      }
+    }
+  }
+#pragma unroll
+  for (int m = 0; m < E; ++m) sm_st<LCG>(sm, rowbase + ((uint32_t)m << ls), cg, x[m]);
+}
+
+template <int ET, int LCG>
+__device__ __forceinline__ void substep_any(int et, uint4* sm, const uint32_t* __restrict__ twt, uint32_t rowbase,
+                                            uint32_t cg, int ls, int s0, uint32_t low) {
+  if constexpr (ET >= 1) {
+    if (et == ET) {
+      substep<ET, LCG>(sm, twt, rowbase, cg, ls, s0, low);
+      return;
+    }
+    substep_any<ET - 1, LCG>(et, sm, twt, rowbase, cg, ls, s0, low);
+  }
+}
+
+__device__ __forceinline__ uint32_t brev(uint32_t x, int bits) { return bits == 0 ? 0u : (__brev(x) >> (32 - bits)); }
+
+}  // namespace p32
+
+template <int ET, int LCG>
+__global__ void __launch_bounds__(512) ntt_p32_kernel(P32Args A) {
+  using namespace p32;
+  extern __shared__ uint4 gsn_smem[];
+  uint4* sm = gsn_smem;
+  constexpr uint32_t CG = 1u << LCG;
+  const int r = A.log_r;
+  const uint32_t R = 1u << r;
+  const int lj = A.log_j;  // == LCG + 2
+
+  for (uint64_t tile = blockIdx.x; tile < A.tiles; tile += gridDim.x) {
+    // --- tile geometry (see ntt_tile) ---
+    uint64_t base = 0, jbase = 0, rowpre = 0, obase = 0;
+    int lo0 = 0;
+    if (!A.last) {
+      const int per_prefix_log = A.log_inner - lj;
+      const uint64_t prefix = tile >> per_prefix_log;
+      jbase = (tile & (((uint64_t)1 << per_prefix_log) - 1)) << lj;
+      base = (prefix << (r + A.log_inner)) + jbase;
+    } else {
+      lo0 = (A.npass == 1) ? 0 : A.radix_log[0];
+      const int k0b_log = lo0 - lj;
+      const uint64_t rest = tile >> k0b_log;
+      const uint64_t k0 = (tile & (((uint64_t)1 << k0b_log) - 1)) << lj;
+      rowpre = (k0 << (A.log_outer - lo0)) + rest;
+      obase = k0 + (rest_offset(rest, A.npass, A.radix_log) << lo0);
+    }
+
+    // --- load: global -> shared ---
+    if (!A.last) {
+      for (uint32_t v = threadIdx.x; v < R * CG; v += blockDim.x) {
+        const uint32_t k = v >> LCG, cg = v & (CG - 1);
+        const uint64_t g = base + ((uint64_t)k << A.log_inner) + 4 * cg;
+        uint4 x = __ldcg(reinterpret_cast<const uint4*>(A.src + g));
+        if (A.first) x = premul(A, x, g);
+        sm_st<LCG>(sm, k, cg, x);
+      }
+    } else {
+      const int row_stride_log = A.log_outer - lo0;
+      for (uint32_t v = threadIdx.x; v < (R >> 2) * CG; v += blockDim.x) {
+        const uint32_t jg = v & (CG - 1), k4 = v >> LCG;
+        uint4 rr[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const uint64_t jj = 4 * jg + i;
+          const uint64_t g = ((rowpre + (jj << row_stride_log)) << r) + 4 * k4;
+          rr[i] = __ldcg(reinterpret_cast<const uint4*>(A.src + g));
+          if (A.first) rr[i] = premul(A, rr[i], g);
+        }
+        sm_st<LCG>(sm, 4 * k4 + 0, jg, make_uint4(rr[0].x, rr[1].x, rr[2].x, rr[3].x));
+        sm_st<LCG>(sm, 4 * k4 + 1, jg, make_uint4(rr[0].y, rr[1].y, rr[2].y, rr[3].y));
+        sm_st<LCG>(sm, 4 * k4 + 2, jg, make_uint4(rr[0].z, rr[1].z, rr[2].z, rr[3].z));
+        sm_st<LCG>(sm, 4 * k4 + 3, jg, make_uint4(rr[0].w, rr[1].w, rr[2].w, rr[3].w));
+      }
+    }
+    __syncthreads();
+
+    // --- radix-2^ET register sub-steps (DIF; bit-reversed order in the tile) ---
+    for (int s0 = 0; s0 < r;) {
+      const int et = (r - s0 < ET) ? (r - s0) : ET;
+      const int ls = r - s0 - et;
+      const uint32_t units = (R >> et) * CG;
+      for (uint32_t u = threadIdx.x; u < units; u += blockDim.x) {
+        const uint32_t cg = u & (CG - 1);
+        const uint32_t uu = u >> LCG;
+        const uint32_t low = uu & ((1u << ls) - 1u);
+        const uint32_t b = uu >> ls;
+        substep_any<ET, LCG>(et, sm, A.tw_tile, (b << (r - s0)) + low, cg, ls, s0, low);
+      }
+      __syncthreads();
+      s0 += et;
+    }
+
+    // --- four-step twiddle (or post table) and store ---
+    for (uint32_t v = threadIdx.x; v < R * CG; v += blockDim.x) {
+      const uint32_t k = v >> LCG, cg = v & (CG - 1);
+      uint4 x = sm_ld<LCG>(sm, brev(k, r), cg);
+      if (!A.last) {
+        const uint64_t jp = jbase + 4 * cg;
+        const uint64_t ek = (uint64_t)k << A.log_outer;
+        uint4 w;
+        w.x = tw_n(A, jp * ek);
+        w.y = tw_n(A, (jp + 1) * ek);
+        w.z = tw_n(A, (jp + 2) * ek);
+        w.w = tw_n(A, (jp + 3) * ek);
+        x = mul4v(x, w);
+        *reinterpret_cast<uint4*>(A.dst + base + ((uint64_t)k << A.log_inner) + 4 * cg) = x;
+      } else {
+        const uint64_t opos = obase + 4 * cg + ((uint64_t)k << A.log_outer);
+        if (A.post_table) x = mul4v(x, __ldg(reinterpret_cast<const uint4*>(A.post_table + opos)));
+        *reinterpret_cast<uint4*>(A.dst + opos) = x;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+struct P32Kernels {
+  template <int ET, int LCG>
+  static cudaError_t launch_one(const P32Args& A, int block, int grid_cap, cudaStream_t s) {
+    const size_t smem = ((size_t)1 << (A.log_r + A.log_j)) * sizeof(uint32_t);
+    auto k = ntt_p32_kernel<ET, LCG>;
+    if (smem > 48 * 1024) {
+      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) return e;
+    }
+    const uint64_t grid = A.tiles < (uint64_t)grid_cap ? A.tiles : (uint64_t)grid_cap;
+    k<<<(unsigned)grid, block, smem, s>>>(A);
+    return cudaGetLastError();
+  }
+  static cudaError_t launch(const P32Args& A, int e_log, int block, int grid_cap, cudaStream_t s) {
+    const int lcg = A.log_j - 2;
+    if (e_log == 3) {
+      if (lcg == 0) return launch_one<3, 0>(A, block, grid_cap, s);
+      if (lcg == 1) return launch_one<3, 1>(A, block, grid_cap, s);
+      if (lcg == 2) return launch_one<3, 2>(A, block, grid_cap, s);
+    } else if (e_log == 4) {
+      if (lcg == 0) return launch_one<4, 0>(A, block, grid_cap, s);
+      if (lcg == 1) return launch_one<4, 1>(A, block, grid_cap, s);
+      if (lcg == 2) return launch_one<4, 2>(A, block, grid_cap, s);
+    }
+    return cudaErrorInvalidValue;
+  }
+};
+
+}  // namespace gsn

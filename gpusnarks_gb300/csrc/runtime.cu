@@ -93,6 +93,14 @@ size_t plan_smem_bytes(const FieldOps& F, const Plan& p, int pass) {
 
 bool plan_valid(const FieldOps& F, const Plan& p) {
   if (p.npass < 1 || p.npass > kMaxPasses) return false;
+  if (p.kernel == kKernelP32) {
+    // 16-byte vectors along 4..16 columns, at least two passes, radix >= 4
+    if (F.id != GSN_P32 || p.npass < 2 || (p.e_log != 3 && p.e_log != 4)) return false;
+    for (int i = 0; i < p.npass; ++i)
+      if (p.log_j[i] < 2 || p.log_j[i] > 4 || p.radix_log[i] < 2 || p.block[i] > 512) return false;
+  } else if (p.kernel != kKernelGeneric) {
+    return false;
+  }
   int sum = 0;
   for (int i = 0; i < p.npass; ++i) {
     if (p.radix_log[i] < 0 || p.log_j[i] < 0) return false;
@@ -153,9 +161,38 @@ bool get_tuned_plan(int field, int log_n, Plan* out) {
   return true;
 }
 
-Plan plan_for(const FieldOps& F, int log_n) {
+// Register-blocked 32-bit plan: passes of radix <= 2^max_r over tiles of
+// 2^log_j columns, 2^e_log rows per thread per register sub-step.
+Plan make_p32_plan(int log_n, int max_r, int log_j, int e_log) {
   Plan p;
-  if (get_tuned_plan(F.id, log_n, &p) && plan_valid(F, p)) return p;
+  p.log_n = log_n;
+  p.kernel = kKernelP32;
+  p.e_log = e_log;
+  p.npass = std::max(2, (log_n + max_r - 1) / max_r);
+  if (p.npass > kMaxPasses) p.npass = kMaxPasses;
+  const int base = log_n / p.npass, extra = log_n % p.npass;
+  for (int i = 0; i < p.npass; ++i) p.radix_log[i] = base + (i < extra ? 1 : 0);
+  for (int i = 0; i < p.npass; ++i) {
+    const bool last = i == p.npass - 1;
+    int inner = 0;
+    for (int k = i + 1; k < p.npass; ++k) inner += p.radix_log[k];
+    const int lj = std::min(log_j, last ? p.radix_log[0] : inner);
+    p.log_j[i] = lj;
+    int threads = (1 << (p.radix_log[i] + lj)) >> (2 + e_log);
+    threads = std::max(32, std::min(512, threads));
+    p.block[i] = threads;
+  }
+  return p;
+}
+
+Plan plan_for(const FieldOps& F, int log_n, bool batched) {
+  Plan p;
+  if (get_tuned_plan(F.id, log_n, &p) && plan_valid(F, p) && !(batched && p.kernel != kKernelGeneric)) return p;
+  if (F.id == GSN_P32 && !batched && log_n >= 8) {
+    // tiles of at most 2^14 elements (64 KB): J = 8 columns, radix <= 2^11
+    p = make_p32_plan(log_n, 11, 3, 4);
+    if (plan_valid(F, p)) return p;
+  }
   FieldLimits L = limits_of(F);
   return make_plan(F, log_n, L.max_r, L.target_j, L.max_block);
 }
@@ -275,6 +312,7 @@ int resolve_tables(const FieldOps& F, uint32_t log_n, const uint32_t* omega, int
     rc = powers_table(F, omega, (int)log_n, &T->tw);
   }
   if (rc) return rc;
+  std::memcpy(T->root, omega ? omega : def, sizeof(uint32_t) * N);
   T->inverse = (dir == GSN_INVERSE || dir == GSN_COSET_INVERSE) ? 1 : 0;
   T->has_pre_const = 0;
   T->pre_table = nullptr;
@@ -313,6 +351,26 @@ int resolve_tables(const FieldOps& F, uint32_t log_n, const uint32_t* omega, int
   return GSN_OK;
 }
 
+int resolve_p32_tables(const FieldOps& F, const Plan& plan, Tables* T) {
+  uint32_t root[kMaxLimbs];
+  std::memcpy(root, T->root, sizeof(uint32_t) * F.limbs);
+  if (T->inverse) F.inv(T->root, root);
+  const int L = plan.log_n;
+  for (int p = 0; p < plan.npass; ++p) {
+    const int r = plan.radix_log[p];
+    uint32_t wr[kMaxLimbs];
+    F.pow(root, (uint64_t)1 << (L - r), wr);  // a primitive 2^r-th root
+    int rc = powers_table(F, wr, r - 1, &T->p32_tile[p]);
+    if (rc) return rc;
+  }
+  T->p32_lo_bits = (L + 1) / 2;
+  int rc = powers_table(F, root, T->p32_lo_bits, &T->p32_lo);
+  if (rc) return rc;
+  uint32_t hb[kMaxLimbs];
+  F.pow(root, (uint64_t)1 << T->p32_lo_bits, hb);
+  return powers_table(F, hb, L - T->p32_lo_bits, &T->p32_hi);
+}
+
 int scratch_for(cudaStream_t s, size_t bytes, uint32_t** out) {
   TableCache& C = cache();
   std::lock_guard<std::mutex> g(C.mu);
@@ -332,8 +390,49 @@ int scratch_for(cudaStream_t s, size_t bytes, uint32_t** out) {
   return GSN_OK;
 }
 
+static int enqueue_p32(const Plan& plan, const Tables& T, uint32_t* data, uint32_t* scratch, cudaStream_t s) {
+  static int sms = 0;
+  if (!sms) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (sms <= 0) sms = 152;
+  }
+  P32Args A;
+  std::memset(&A, 0, sizeof(A));
+  A.tw_lo = T.p32_lo;
+  A.tw_hi = T.p32_hi;
+  A.lo_bits = T.p32_lo_bits;
+  A.log_n = plan.log_n;
+  A.npass = plan.npass;
+  for (int i = 0; i < kMaxPasses; ++i) A.radix_log[i] = plan.radix_log[i];
+  int outer = 0;
+  for (int p = 0; p < plan.npass; ++p) {
+    A.first = p == 0;
+    A.last = p == plan.npass - 1;
+    A.src = A.first ? data : scratch;
+    A.dst = A.last ? data : scratch;
+    A.tw_tile = T.p32_tile[p];
+    A.log_r = plan.radix_log[p];
+    A.log_outer = outer;
+    A.log_inner = plan.log_n - outer - plan.radix_log[p];
+    A.log_j = plan.log_j[p];
+    A.tiles = (uint64_t)1 << (plan.log_n - A.log_r - A.log_j);
+    A.pre_table = A.first ? T.pre_table : nullptr;
+    A.post_table = A.last ? T.post_table : nullptr;
+    A.has_pre_const = A.first ? T.has_pre_const : 0;
+    A.pre_const = T.pre_const[0];
+    cudaError_t e = launch_p32_pass(A, plan.e_log, plan.block[p], sms * 16, s);
+    if (e != cudaSuccess) return cuda_fail(e, "p32 NTT pass launch");
+    count_launches(1);
+    outer += plan.radix_log[p];
+  }
+  return GSN_OK;
+}
+
 int enqueue_ntt(const FieldOps& F, const Plan& plan, const Tables& T, uint32_t* data, uint32_t* scratch,
                 cudaStream_t s) {
+  if (plan.kernel == kKernelP32) return enqueue_p32(plan, T, data, scratch, s);
   PassArgs A;
   std::memset(&A, 0, sizeof(A));
   A.tw = T.tw;
@@ -383,6 +482,10 @@ static int ntt_impl(int field, uint32_t* data, uint32_t log_n, const uint32_t* o
   rc = resolve_tables(*F, log_n, omega, dir, shift, &T, s);
   if (rc) return rc;
   Plan plan = plan_for(*F, (int)log_n);
+  if (plan.kernel == kKernelP32) {
+    rc = resolve_p32_tables(*F, plan, &T);
+    if (rc) return rc;
+  }
   if (plan.npass > 1 && !scratch) {
     rc = scratch_for(s, ((size_t)1 << log_n) * F->limbs * sizeof(uint32_t), &scratch);
     if (rc) return rc;

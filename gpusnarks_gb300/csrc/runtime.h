@@ -25,18 +25,27 @@ int cuda_fail(cudaError_t e, const char* what);
 
 void count_launches(uint64_t n);
 
-// A transform plan: pass split, tile shape and threads per pass.
+// A transform plan: pass split, tile shape and threads per pass, and which
+// kernel runs the passes.
+enum PlanKernel { kKernelGeneric = 0, kKernelP32 = 1 };
+
 struct Plan {
   int log_n = 0;
   int npass = 0;
   int radix_log[kMaxPasses] = {0, 0, 0, 0};
   int log_j[kMaxPasses] = {0, 0, 0, 0};
   int block[kMaxPasses] = {0, 0, 0, 0};
+  int kernel = kKernelGeneric;  // kKernelP32: register-blocked 32-bit pass (ntt_p32.cuh)
+  int e_log = 4;                // kKernelP32: rows per thread per register sub-step (log2)
 };
+
+// Register-blocked 32-bit pass launcher (ntt_f_p32.cu).
+cudaError_t launch_p32_pass(const P32Args& A, int e_log, int block, int grid_cap, cudaStream_t s);
 
 // Default plan for (field, log_n), or the tuned one when a tuning table is
 // loaded.
-Plan plan_for(const FieldOps& F, int log_n);
+Plan plan_for(const FieldOps& F, int log_n, bool batched = false);
+Plan make_p32_plan(int log_n, int max_r, int log_j, int e_log);
 // Heuristic plan with explicit limits (used by the autotuner's candidate set).
 Plan make_plan(const FieldOps& F, int log_n, int max_r, int target_j, int max_block);
 bool plan_valid(const FieldOps& F, const Plan& p);
@@ -54,7 +63,16 @@ struct Tables {
   int has_pre_const = 0;
   uint32_t pre_const[kMaxLimbs] = {0};
   int inverse = 0;
+  uint32_t root[kMaxLimbs] = {0};  // canonical root actually used (omega^-1 when inverse)
+  // register-blocked 32-bit pass tables, filled by resolve_p32_tables
+  const uint32_t* p32_tile[kMaxPasses] = {nullptr, nullptr, nullptr, nullptr};
+  const uint32_t* p32_lo = nullptr;
+  const uint32_t* p32_hi = nullptr;
+  int p32_lo_bits = 0;
 };
+
+// Compact per-radix and two-level four-step tables for a kKernelP32 plan.
+int resolve_p32_tables(const FieldOps& F, const Plan& plan, Tables* T);
 
 // Validates arguments and resolves (and caches) all tables for a transform.
 int resolve_tables(const FieldOps& F, uint32_t log_n, const uint32_t* omega, int dir, const uint32_t* shift,
