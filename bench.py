@@ -1,0 +1,401 @@
+"""Benchmark: field NTT on one GB300 (per rank), one JSON line on rank 0.
+
+Headline workload (``value``): forward NTT over the MNT4-753 scalar field r
+(24 x 32-bit limbs), n = 2^18, seeded uniform inputs, data resident in HBM;
+the input (25 MB) is smaller than L2, so L2 is flushed (256 MB write) before
+every timed step and only the transform is timed, with CUDA events on the
+launching stream.  ``e2e`` is the same transform through the C-ABI host entry
+point gsn_ntt_host (the best_fft drop-in) from pinned host memory, copies
+included.  ``roofline`` compares the transform's algorithmic integer
+multiply-adds (2352 per 24-limb Montgomery product, (n/2) log2 n products)
+with the measured throughput of the same PTX carry-chain instructions
+(gsn_microbench_imad) in the same process.
+
+``extra`` carries the other configurations (32-bit sweep against the HBM
+roofline, MNT4 2^20, the 4096-job BLS12-381 batch against per-call, serving
+p50/p99) unless --headline-only.
+
+--impl reference times the reference's host FFT algorithm (the oracle's
+restatement of test/fft_host.h, fixed butterfly, OpenMP over all host cores)
+on the same workload; it is the CPU arm the driver compares against.
+
+Multi-GPU: the path shards by independent transforms (replicas); under
+torchrun every rank runs the workload on its own GPU and rank 0 reports the
+max time over ranks (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import math
+import os
+import pathlib
+import shutil
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = pathlib.Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "field-NTT Melem/s & % roofline, batched vs per-call; serving p50/p99 latency"
+HEADLINE_LOG_N = 18
+SEED = 0x5EED0000
+PEAKS = ROOT / "MEASURED_PEAKS.json"
+PUBLISHED_REF_768_2_18_S = 21.42  # README.md:46, GTX 1060, the reference's own (non-DFT) dataflow
+
+
+# --------------------------------------------------------------------------- utils
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+    return rank, local, ws
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, ws: int) -> float:
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi samples during the timed region (SM clock, throttle reasons)."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        if shutil.which("nvidia-smi"):
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self) -> dict:
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def peaks() -> dict:
+    try:
+        return json.loads(PEAKS.read_text())
+    except Exception:
+        return {}
+
+
+# --------------------------------------------------------------------------- GPU arm
+def imad_peak(g) -> dict:
+    lib = g.load()
+    a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+    g._lib.check(lib.gsn_microbench_imad(20000, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+    return {"mads_per_s": a.value, "mads_per_clk_sm": b.value, "sm_mhz": c.value}
+
+
+def time_device_ntt(g, torch, f, log_n: int, steps: int, warmup: int, direction=0, flush=None):
+    """Per-step CUDA-event time of one in-place transform (L2 flushed before each)."""
+    n = 1 << log_n
+    data = torch.empty(n * f.limbs, dtype=torch.int32, device="cuda")
+    from gpusnarks_gb300.batch import fill_random
+    fill_random(f, data, SEED + log_n)
+    stream = torch.cuda.current_stream()
+    for _ in range(warmup):
+        g.ntt(f, data, direction=direction)
+    torch.cuda.synchronize()
+    times = []
+    launches0 = g.launch_count()
+    for _ in range(steps):
+        if flush is not None:
+            flush.zero_()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        g.ntt(f, data, direction=direction)
+        e.record(stream)
+        e.synchronize()
+        times.append(s.elapsed_time(e) * 1e-3)
+    launches = g.launch_count() - launches0
+    del data
+    return times, launches
+
+
+def time_e2e_host(g, f, log_n: int, steps: int, warmup: int):
+    """gsn_ntt_host on pinned host memory: H2D + transform + D2H per step."""
+    n = 1 << log_n
+    nbytes = n * f.limbs * 4
+    buf = g.host_buffer(nbytes)
+    arr = np.ctypeslib.as_array(ctypes.cast(buf, ctypes.POINTER(ctypes.c_uint32)), shape=(n * f.limbs,))
+    arr[:] = f.device_random(n, SEED + log_n).reshape(-1)
+    lib = g.load()
+    for _ in range(warmup):
+        g._lib.check(lib.gsn_ntt_host(f.fid, buf.value, log_n, None, 0, None))
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        g._lib.check(lib.gsn_ntt_host(f.fid, buf.value, log_n, None, 0, None))
+        times.append(time.perf_counter() - t0)
+    g.free_host_buffer(buf)
+    return times, nbytes
+
+
+def imad_work(f, log_n: int) -> float:
+    s = f.limbs
+    per_mul = 2 * (2 * s * s + s)
+    return per_mul * (2 ** (log_n - 1)) * log_n
+
+
+def p32_sweep(g, torch, flush, hbm_gbs, steps=5):
+    out = {}
+    l2 = torch.cuda.get_device_properties(0).L2_cache_size
+    for log_n in (20, 22, 24, 26, 28):
+        n = 1 << log_n
+        ts, _ = time_device_ntt(g, torch, g.P32, log_n, steps, 2, flush=flush)
+        t = float(np.median(ts))
+        pmin = 1 if 4 * n <= l2 / 2 else 2
+        B = 2 * 4 * n * pmin
+        out[f"2^{log_n}"] = {"ms": round(t * 1e3, 4), "Melem_s": round(n / t / 1e6, 1),
+                             "hbm_frac": round(B / t / 1e9 / hbm_gbs, 4),
+                             "single_pass_frac": round(8 * n / t / 1e9 / hbm_gbs, 4), "p_min": pmin}
+    return out
+
+
+def batch_vs_per_call(g, torch, njobs=4096, lo=10, hi=20, reps=3):
+    from gpusnarks_gb300.batch import Batch, fill_random, job_sizes
+    f = g.BLS12_381
+    sizes = job_sizes(njobs, lo, hi, SEED + 4)
+    total = sum(1 << k for k in sizes)
+    pool = torch.empty(total * f.limbs, dtype=torch.int32, device="cuda")
+    fill_random(f, pool, SEED + 4)
+    jobs, off = [], 0
+    for k in sizes:
+        jobs.append((pool.data_ptr() + off * f.limbs * 4, k, 0, None, None))
+        off += 1 << k
+    b = Batch(f, jobs, graph=True)
+    stream = torch.cuda.current_stream()
+
+    def timed(fn):
+        ts = []
+        for _ in range(reps):
+            torch.cuda.synchronize()
+            s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s.record(stream)
+            fn()
+            e.record(stream)
+            e.synchronize()
+            ts.append(s.elapsed_time(e) * 1e-3)
+        return float(np.median(ts))
+
+    b.launch()
+    b.launch_per_call()
+    torch.cuda.synchronize()
+    t_batch = timed(lambda: b.launch())
+    b.status()
+    t_call = timed(lambda: b.launch_per_call())
+    info = b.info()
+    b.close()
+    del pool
+    torch.cuda.empty_cache()
+    work = sum(imad_work(f, k) for k in sizes)
+    return {"jobs": njobs, "elements": total, "log_n_range": [lo, hi],
+            "batched_ms": round(t_batch * 1e3, 3), "per_call_ms": round(t_call * 1e3, 3),
+            "batched_Melem_s": round(total / t_batch / 1e6, 1), "per_call_Melem_s": round(total / t_call / 1e6, 1),
+            "speedup": round(t_call / t_batch, 3), "batched_imad_T_s": round(work / t_batch / 1e12, 3),
+            "work_items": info["work_items"]}
+
+
+def run_gpu(args, rank, local, ws):
+    import torch
+
+    import gpusnarks_gb300 as g
+    torch.cuda.set_device(local)
+    g.load()
+    f = g.MNT4_753
+    log_n = HEADLINE_LOG_N
+    n = 1 << log_n
+    flush = torch.empty(256 << 20, dtype=torch.int8, device="cuda")
+    pk = peaks()
+    hbm_gbs = float(pk.get("hbm_gbs", 6800.0))
+    ip = imad_peak(g)
+
+    # headline: device-resident transforms
+    barrier(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        ts, launches = time_device_ntt(g, torch, f, log_n, args.steps, args.warmup, flush=flush)
+    torch.cuda.synchronize()
+    barrier(ws)
+    t_total = max_over_ranks(sum(ts), ws)
+    t_step = t_total / args.steps
+    value = n * args.steps * ws / t_total / 1e6
+    achieved = imad_work(f, log_n) / t_step
+
+    # e2e through the host entry point
+    e2e_ts, nbytes = time_e2e_host(g, f, log_n, args.steps, max(1, args.warmup // 2))
+    e2e_t = max_over_ranks(float(np.mean(e2e_ts)), ws)
+
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": "Melem/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "forward NTT, MNT4-753 scalar field r (24 limbs), n=2^18, per GPU",
+                   "field": "mnt4753_fr", "log_n": log_n, "elements_per_step": n,
+                   "l2": "flushed (256 MB write) before each step; input 25 MB < L2",
+                   "parallelism": f"replicas x{ws}"},
+        "e2e": {"value": round(n * ws / e2e_t / 1e6, 3), "unit": "Melem/s", "h2d_bytes_per_step": nbytes,
+                "d2h_bytes_per_step": nbytes, "api": "gsn_ntt_host (pinned host buffer)"},
+        "roofline": {"bound": "imad", "achieved": round(achieved / 1e12, 4),
+                     "peak": round(ip["mads_per_s"] / 1e12, 4), "unit": "TIMAD/s",
+                     "frac": round(achieved / ip["mads_per_s"], 4), "traffic": None,
+                     "peak_source": "gsn_microbench_imad in this process (PTX mad.lo.cc/madc.hi.cc chains, "
+                                    "all SMs, full occupancy)",
+                     "algorithmic_work": "2352 IMAD per 24-limb Montgomery product x (n/2) log2 n"},
+        "gpu_launches": int(launches),
+        "clocks": clk.summary(),
+        "published_reference": {"what": "FFT 768-bit n=2^18, GTX 1060, reference dataflow (not a DFT)",
+                                "seconds": PUBLISHED_REF_768_2_18_S,
+                                "Melem_s": round(n / PUBLISHED_REF_768_2_18_S / 1e6, 5)},
+    }
+    trf = ROOT / "profiles" / "traffic.json"
+    if trf.exists():
+        try:
+            line["roofline"]["traffic"] = json.loads(trf.read_text()).get("mnt4753_fr_2^18_bytes_per_step")
+        except Exception:
+            pass
+    if rank == 0 and ws == 1:
+        line["cpu_baseline"] = cpu_baseline(args)
+    if not args.headline_only and rank == 0:
+        extra = {}
+        t20, _ = time_device_ntt(g, torch, f, 20, 3, 1, flush=flush)
+        extra["mnt4753_fr_2^20"] = {"ms": round(float(np.median(t20)) * 1e3, 3),
+                                    "imad_frac": round(imad_work(f, 20) / float(np.median(t20)) / ip["mads_per_s"], 4)}
+        extra["p32_sweep"] = p32_sweep(g, torch, flush, hbm_gbs)
+        extra["hbm_peak_gbs"] = hbm_gbs
+        try:
+            extra["bls12_381_batch_4096"] = batch_vs_per_call(g, torch)
+        except Exception as exc:  # report, do not hide
+            extra["bls12_381_batch_4096"] = {"error": str(exc)}
+        try:
+            from gpusnarks_gb300.serve import bench_serving
+            extra["serving"] = bench_serving(g, torch, seconds=args.serve_seconds)
+        except Exception as exc:
+            extra["serving"] = {"error": str(exc)}
+        extra["imad_microbench"] = ip
+        line["extra"] = extra
+    return line
+
+
+# --------------------------------------------------------------------------- CPU arm
+def cpu_baseline(args) -> dict:
+    """The oracle's restatement of the reference host FFT on this host's cores."""
+    import oracle
+    import gpusnarks_gb300.fields as fields
+    f = fields.MNT4_753
+    n = 1 << HEADLINE_LOG_N
+    x = f.device_random(n, SEED + HEADLINE_LOG_N)
+    threads = os.cpu_count() or 1
+    log_cpus = max(0, int(math.floor(math.log2(threads))))
+    w = oracle.root(2, HEADLINE_LOG_N)
+    oracle.fft(2, x, w, log_cpus=log_cpus, nthreads=threads)  # warm
+    reps, ts = 0, []
+    t_start = time.perf_counter()
+    while reps < args.cpu_reps or (time.perf_counter() - t_start < 10 and reps < 20):
+        t0 = time.perf_counter()
+        oracle.fft(2, x, w, log_cpus=log_cpus, nthreads=threads)
+        ts.append(time.perf_counter() - t0)
+        reps += 1
+    t = float(np.median(ts))
+    return {"value": round(n / t / 1e6, 5), "unit": "Melem/s", "cores": threads, "kind": "port",
+            "sample": f"full n=2^18 MNT4-753 r transform x{reps} (median), num_cpus decomposition "
+                      f"log_cpus={log_cpus}, {threads} OpenMP threads; oracle/oracle.cpp restating "
+                      "test/fft_host.h with the fixed butterfly"}
+
+
+def run_reference(args, rank, ws):
+    if rank != 0:
+        return None
+    cb = cpu_baseline(args)
+    v = cb["value"]
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "Melem/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round((1 << HEADLINE_LOG_N) / v / 1e3, 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+            "config": {"workload": "forward NTT, MNT4-753 scalar field r (24 limbs), n=2^18",
+                       "field": "mnt4753_fr", "log_n": HEADLINE_LOG_N},
+            "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--headline-only", action="store_true")
+    ap.add_argument("--cpu-reps", type=int, default=3)
+    ap.add_argument("--serve-seconds", type=float, default=1.0)
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    rank, local, ws = dist_init()
+    if args.impl == "reference":
+        line = run_reference(args, rank, ws)
+    else:
+        line = run_gpu(args, rank, local, ws)
+    if rank == 0 and line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

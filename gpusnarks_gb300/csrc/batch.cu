@@ -53,6 +53,64 @@ static void batch_free(gsn_batch* b) {
   delete b;
 }
 
+uint64_t job_scratch_bytes(const FieldOps& F, const Plan& p) {
+  return p.npass > 1 ? ((uint64_t)1 << p.log_n) * F.limbs * sizeof(uint32_t) : 0;
+}
+
+int plan_batch(const FieldOps& F, const gsn_batch_job* jobs, size_t njobs, BatchPlan* out) {
+  const uintptr_t align = (F.limbs % 4 == 0) ? 16 : 4;
+  out->plans.resize(njobs);
+  out->jobs.resize(njobs);
+  out->work.clear();
+  out->block = 0;
+  out->smem = 0;
+  out->elements = 0;
+  for (size_t i = 0; i < njobs; ++i) {
+    const gsn_batch_job& u = jobs[i];
+    if (!u.data || reinterpret_cast<uintptr_t>(u.data) % align)
+      return set_error(GSN_ERR_ARG, "job %zu: null or misaligned data pointer", i);
+    Tables T;
+    int rc = resolve_tables(F, u.log_n, u.omega, u.dir, u.shift, &T, nullptr);
+    if (rc) return rc;
+    Plan p = plan_for(F, (int)u.log_n, /*batched=*/true);
+    out->plans[i] = p;
+    BatchJob& J = out->jobs[i];
+    std::memset(&J, 0, sizeof(J));
+    J.data = u.data;
+    J.tw = T.tw;
+    J.tw_log = T.tw_log;
+    J.pre_table = T.pre_table;
+    J.post_table = T.post_table;
+    J.log_n = (int)u.log_n;
+    J.inverse = T.inverse;
+    J.npass = p.npass;
+    for (int k = 0; k < kMaxPasses; ++k) {
+      J.radix_log[k] = p.radix_log[k];
+      J.log_j[k] = p.log_j[k];
+    }
+    J.has_pre_const = T.has_pre_const;
+    std::memcpy(J.pre_const, T.pre_const, sizeof(J.pre_const));
+    out->elements += (uint64_t)1 << u.log_n;
+    for (int k = 0; k < p.npass; ++k) {
+      out->block = std::max(out->block, p.block[k]);
+      out->smem = std::max(out->smem, plan_smem_bytes(F, p, k));
+    }
+  }
+  // work queue, by level, largest jobs first within a level
+  std::vector<size_t> order(njobs);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](size_t x, size_t y) { return jobs[x].log_n > jobs[y].log_n; });
+  for (int level = 0; level < kMaxPasses; ++level) {
+    for (size_t i : order) {
+      const Plan& p = out->plans[i];
+      if (level >= p.npass) continue;
+      const uint64_t tiles = (uint64_t)1 << (p.log_n - p.radix_log[level] - p.log_j[level]);
+      for (uint64_t t = 0; t < tiles; ++t) out->work.push_back(((uint64_t)i << 32) | ((uint64_t)level << 28) | t);
+    }
+  }
+  return GSN_OK;
+}
+
 static int enqueue_batch(gsn_batch* b, cudaStream_t s) {
   GSN_CUDA(cudaMemsetAsync(b->counters_dev, 0, b->counters_bytes, s));
   GSN_CUDA(cudaMemsetAsync(b->status_dev, 0, sizeof(uint32_t), s));
@@ -81,77 +139,34 @@ int gsn_batch_create(int field, const gsn_batch_job* jobs, size_t njobs, int fla
   b->user.assign(jobs, jobs + njobs);
   b->plans.resize(njobs);
   b->jobs.resize(njobs);
-  const size_t elt = F->limbs * sizeof(uint32_t);
-  const uintptr_t align = (F->limbs % 4 == 0) ? 16 : 4;
-
-  // plans, tables and scratch layout
-  std::vector<uint64_t> scratch_off(njobs, 0);
-  uint64_t scratch_total = 0;
-  for (size_t i = 0; i < njobs; ++i) {
-    const gsn_batch_job& u = jobs[i];
-    if (!u.data || reinterpret_cast<uintptr_t>(u.data) % align) {
-      batch_free(b);
-      return set_error(GSN_ERR_ARG, "job %zu: null or misaligned data pointer", i);
-    }
-    Tables T;
-    int rc = resolve_tables(*F, u.log_n, u.omega, u.dir, u.shift, &T, nullptr);
-    if (rc) {
-      batch_free(b);
-      return rc;
-    }
-    Plan p = plan_for(*F, (int)u.log_n, /*batched=*/true);
-    b->plans[i] = p;
-    BatchJob& J = b->jobs[i];
-    std::memset(&J, 0, sizeof(J));
-    J.data = u.data;
-    J.tw = T.tw;
-    J.tw_log = T.tw_log;
-    J.pre_table = T.pre_table;
-    J.post_table = T.post_table;
-    J.log_n = (int)u.log_n;
-    J.inverse = T.inverse;
-    J.npass = p.npass;
-    for (int k = 0; k < kMaxPasses; ++k) {
-      J.radix_log[k] = p.radix_log[k];
-      J.log_j[k] = p.log_j[k];
-    }
-    J.has_pre_const = T.has_pre_const;
-    std::memcpy(J.pre_const, T.pre_const, sizeof(J.pre_const));
-    const uint64_t n = (uint64_t)1 << u.log_n;
-    b->elements += n;
-    if (p.npass > 1) {
-      scratch_off[i] = scratch_total;
-      scratch_total += (n * elt + 255) & ~(uint64_t)255;
-    }
-    for (int k = 0; k < p.npass; ++k) {
-      b->block = std::max(b->block, p.block[k]);
-      b->smem = std::max(b->smem, plan_smem_bytes(*F, p, k));
-    }
+  BatchPlan bp;
+  int rc = plan_batch(*F, jobs, njobs, &bp);
+  if (rc) {
+    batch_free(b);
+    return rc;
   }
-  int rc = GSN_OK;
+  b->plans = bp.plans;
+  b->jobs = bp.jobs;
+  b->elements = bp.elements;
+  b->block = bp.block;
+  b->smem = bp.smem;
+  std::vector<uint64_t>& work = bp.work;
+  uint64_t scratch_total = 0;
+  std::vector<uint64_t> scratch_off(njobs, 0);
+  for (size_t i = 0; i < njobs; ++i) {
+    const uint64_t bytes = job_scratch_bytes(*F, b->plans[i]);
+    scratch_off[i] = scratch_total;
+    scratch_total += (bytes + 255) & ~(uint64_t)255;
+  }
   if (scratch_total) rc = dev_alloc((void**)&b->scratch_dev, scratch_total);
   if (rc) {
     batch_free(b);
     return rc;
   }
   for (size_t i = 0; i < njobs; ++i)
-    if (b->plans[i].npass > 1)
+    if (job_scratch_bytes(*F, b->plans[i]))
       b->jobs[i].scratch = reinterpret_cast<uint32_t*>(reinterpret_cast<char*>(b->scratch_dev) + scratch_off[i]);
 
-  // work queue, by level, largest jobs first within a level
-  std::vector<size_t> order(njobs);
-  std::iota(order.begin(), order.end(), 0);
-  std::stable_sort(order.begin(), order.end(),
-                   [&](size_t x, size_t y) { return jobs[x].log_n > jobs[y].log_n; });
-  std::vector<uint64_t> work;
-  for (int level = 0; level < kMaxPasses; ++level) {
-    for (size_t i : order) {
-      const Plan& p = b->plans[i];
-      if (level >= p.npass) continue;
-      const uint64_t tiles = (uint64_t)1 << (p.log_n - p.radix_log[level] - p.log_j[level]);
-      for (uint64_t t = 0; t < tiles; ++t) work.push_back(((uint64_t)i << 32) | ((uint64_t)level << 28) | t);
-    }
-  }
   b->nwork = work.size();
   b->counters_bytes = (1 + njobs * kMaxPasses) * sizeof(uint32_t);
   rc = dev_alloc((void**)&b->jobs_dev, njobs * sizeof(BatchJob));

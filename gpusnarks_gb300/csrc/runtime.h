@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "field_ops.h"
+#include "gpusnarks_gb300.h"
 #include "ntt_common.h"
 
 namespace gsn {
@@ -81,6 +82,20 @@ int resolve_tables(const FieldOps& F, uint32_t log_n, const uint32_t* omega, int
 // Enqueues the passes of one transform.
 int enqueue_ntt(const FieldOps& F, const Plan& plan, const Tables& T, uint32_t* data, uint32_t* scratch,
                 cudaStream_t s);
+
+// Host-side plan of one batch: per-job device descriptors (scratch left
+// null for the caller to assign), the tile work list ordered by pass level,
+// and the block / shared memory the persistent kernel needs.
+struct BatchPlan {
+  std::vector<Plan> plans;
+  std::vector<BatchJob> jobs;
+  std::vector<uint64_t> work;
+  int block = 0;
+  size_t smem = 0;
+  uint64_t elements = 0;
+};
+int plan_batch(const FieldOps& F, const struct gsn_batch_job* jobs, size_t njobs, BatchPlan* out);
+uint64_t job_scratch_bytes(const FieldOps& F, const Plan& p);
 
 // Library-owned per-stream scratch (grow-only).
 int scratch_for(cudaStream_t s, size_t bytes, uint32_t** out);

@@ -1,0 +1,172 @@
+"""Serving: Python handle on the native request loop (gsn_server_*).
+
+The scheduler, admission, batching and copies all run in the native library;
+this module builds requests and traces and reads results.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from ._lib import check, load
+
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_int32),
+                ("max_batch_jobs", ctypes.c_int32)]
+
+
+class Request(ctypes.Structure):
+    _fields_ = [("field", ctypes.c_int32), ("log_n", ctypes.c_uint32), ("dir", ctypes.c_int32),
+                ("shift", ctypes.c_void_p), ("host_in", ctypes.c_void_p), ("host_out", ctypes.c_void_p)]
+
+
+class TraceEntry(ctypes.Structure):
+    _fields_ = [("arrival_s", ctypes.c_double), ("req", Request)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
+                ("launches", ctypes.c_uint64), ("device_bytes_in_use", ctypes.c_uint64),
+                ("device_bytes_peak", ctypes.c_uint64), ("busy_s", ctypes.c_double)]
+
+
+_SIGS = [
+    ("gsn_server_create", [ctypes.POINTER(ServerConfig), ctypes.POINTER(ctypes.c_void_p)]),
+    ("gsn_server_warmup", [ctypes.c_void_p, ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32]),
+    ("gsn_server_submit", [ctypes.c_void_p, ctypes.POINTER(Request), ctypes.POINTER(ctypes.c_uint64)]),
+    ("gsn_server_wait", [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    ("gsn_server_fetch", [ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p]),
+    ("gsn_server_release", [ctypes.c_void_p, ctypes.c_uint64]),
+    ("gsn_server_get_stats", [ctypes.c_void_p, ctypes.POINTER(ServerStats)]),
+    ("gsn_server_destroy", [ctypes.c_void_p]),
+    ("gsn_server_run_trace", [ctypes.c_void_p, ctypes.POINTER(TraceEntry), ctypes.c_size_t,
+                              ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+]
+
+
+def _lib():
+    lib = load()
+    for name, args in _SIGS:
+        fn = getattr(lib, name)
+        fn.restype = ctypes.c_int
+        fn.argtypes = args
+    return lib
+
+
+class Server:
+    def __init__(self, hbm_budget_bytes: int, max_inflight: int = 4, max_batch_jobs: int = 0):
+        self.lib = _lib()
+        cfg = ServerConfig(hbm_budget_bytes, max_inflight, max_batch_jobs)
+        h = ctypes.c_void_p()
+        check(self.lib.gsn_server_create(ctypes.byref(cfg), ctypes.byref(h)))
+        self.h = h
+        self._keep = []
+
+    def warmup(self, field, lo: int, hi: int) -> None:
+        from . import field_of
+        check(self.lib.gsn_server_warmup(self.h, field_of(field).fid, lo, hi))
+
+    def submit(self, field, host_in: np.ndarray, direction: int = 0, shift=None, host_out: np.ndarray | None = None):
+        from . import _limbs, field_of
+        f = field_of(field)
+        n = host_in.size // f.limbs
+        s = _limbs(f, shift)
+        self._keep += [host_in, host_out, s]
+        req = Request(f.fid, n.bit_length() - 1, direction, None if s is None else s.ctypes.data,
+                      host_in.ctypes.data, None if host_out is None else host_out.ctypes.data)
+        rid = ctypes.c_uint64()
+        check(self.lib.gsn_server_submit(self.h, ctypes.byref(req), ctypes.byref(rid)))
+        return rid.value
+
+    def wait(self, rid: int, timeout_s: float = 60.0) -> float:
+        lat = ctypes.c_double()
+        check(self.lib.gsn_server_wait(self.h, rid, timeout_s, ctypes.byref(lat)))
+        return lat.value
+
+    def fetch(self, rid: int, out: np.ndarray) -> np.ndarray:
+        check(self.lib.gsn_server_fetch(self.h, rid, out.ctypes.data))
+        return out
+
+    def release(self, rid: int) -> None:
+        check(self.lib.gsn_server_release(self.h, rid))
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        check(self.lib.gsn_server_get_stats(self.h, ctypes.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def run_trace(self, entries) -> tuple[np.ndarray, float]:
+        arr = (TraceEntry * len(entries))(*entries)
+        lat = (ctypes.c_double * len(entries))()
+        mk = ctypes.c_double()
+        check(self.lib.gsn_server_run_trace(self.h, arr, len(entries), lat, ctypes.byref(mk)))
+        return np.array(lat[:], dtype=np.float64), mk.value
+
+    def close(self) -> None:
+        if self.h:
+            check(self.lib.gsn_server_destroy(self.h))
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def poisson_trace(count: int, rate: float, seed: int, fields=(1, 2), lo=12, hi=22, dirs=(0, 1, 2)):
+    """Seeded Poisson arrivals (exponential gaps, mean 1/rate), field chosen
+    uniformly from `fields`, log2 size uniform in [lo, hi], direction uniform."""
+    rng = np.random.default_rng(seed)
+    gaps = rng.exponential(1.0 / rate, size=count)
+    t = np.cumsum(gaps) - gaps[0]
+    fs = rng.choice(np.array(fields), size=count)
+    ks = rng.integers(lo, hi + 1, size=count)
+    ds = rng.choice(np.array(dirs), size=count)
+    return [(float(t[i]), int(fs[i]), int(ks[i]), int(ds[i])) for i in range(count)]
+
+
+def bench_serving(g, torch, *, seconds: float = 1.0, rate: float = 2000.0, budget_gb: float = 120.0,
+                  max_inflight: int = 4, seed: int = 0x5EED0005) -> dict:
+    """Config 5: Poisson stream at `rate` req/s for `seconds`, BLS12-381 / MNT4-753
+    50/50, sizes 2^12..2^22, forward / inverse / coset-forward; 120 GB budget."""
+    from . import BY_ID
+    trace = poisson_trace(max(1, int(rate * seconds)), rate, seed)
+    # one pinned input and output buffer per (field, size): inputs are uniform
+    # random elements; outputs of equal-shape requests overwrite each other
+    bufs = {}
+    for _, fid, k, _ in trace:
+        if (fid, k) not in bufs:
+            f = BY_ID[fid]
+            nbytes = (1 << k) * f.limbs * 4
+            pin = g.host_buffer(nbytes)
+            pout = g.host_buffer(nbytes)
+            a = np.ctypeslib.as_array(ctypes.cast(pin, ctypes.POINTER(ctypes.c_uint32)), shape=((1 << k) * f.limbs,))
+            a[:] = f.device_random(1 << k, seed + 97 * k + fid).reshape(-1)
+            bufs[(fid, k)] = (pin, pout)
+    srv = Server(int(budget_gb * (1 << 30)), max_inflight=max_inflight)
+    try:
+        for fid in (1, 2):
+            srv.warmup(fid, 12, 22)
+        entries = []
+        for (t, fid, k, d) in trace:
+            pin, pout = bufs[(fid, k)]
+            entries.append(TraceEntry(t, Request(fid, k, d, None, pin.value, pout.value)))
+        lat, makespan = srv.run_trace(entries)
+        st = srv.stats()
+    finally:
+        srv.close()
+        for pin, pout in bufs.values():
+            g.free_host_buffer(pin)
+            g.free_host_buffer(pout)
+    elements = sum(1 << k for _, _, k, _ in trace)
+    return {"requests": len(trace), "rate_req_s": rate, "arrival_window_s": round(trace[-1][0], 4),
+            "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
+            "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3),
+            "mean_ms": round(float(lat.mean()) * 1e3, 3), "makespan_s": round(makespan, 4),
+            "throughput_req_s": round(len(trace) / makespan, 1),
+            "throughput_Melem_s": round(elements / makespan / 1e6, 2),
+            "launches": st["launches"], "device_bytes_peak": st["device_bytes_peak"],
+            "budget_bytes": int(budget_gb * (1 << 30)), "max_inflight": max_inflight}

@@ -133,6 +133,64 @@ int gsn_batch_status(gsn_batch* b);
 int gsn_batch_info(gsn_batch* b, uint64_t* njobs, uint64_t* nwork, uint64_t* elements, uint64_t* device_bytes);
 int gsn_batch_destroy(gsn_batch* b);
 
+/* ---- serving (no reference counterpart) -----------------------------------
+ * A request loop that admits forward / inverse / coset NTT jobs of mixed
+ * fields and sizes under an HBM budget, keeps polynomials and twiddle tables
+ * resident on the device, and feeds whatever is ready into the persistent
+ * batch kernel; several launches are in flight at once, so requests that
+ * arrive while others run start as soon as memory and a launch slot free up. */
+
+typedef struct gsn_server gsn_server; /* opaque */
+
+typedef struct gsn_server_config {
+  uint64_t hbm_budget_bytes; /* device bytes for polynomials + scratch            */
+  int32_t max_inflight;      /* persistent launches in flight at once (>= 1)      */
+  int32_t max_batch_jobs;    /* cap on requests per launch (0 = 4096)             */
+} gsn_server_config;
+
+typedef struct gsn_request {
+  int32_t field;
+  uint32_t log_n;
+  int32_t dir;              /* gsn_dir                                          */
+  const uint32_t* shift;    /* coset shift (canonical) or NULL = generator      */
+  const uint32_t* host_in;  /* input, host memory (pinned for full speed)       */
+  uint32_t* host_out;       /* output host memory, or NULL: the result stays
+                               resident until gsn_server_fetch / _release       */
+} gsn_request;
+
+typedef struct gsn_server_stats {
+  uint64_t submitted, completed, failed, launches;
+  uint64_t device_bytes_in_use, device_bytes_peak;
+  double busy_s; /* wall time with at least one launch in flight */
+} gsn_server_stats;
+
+int gsn_server_create(const gsn_server_config* cfg, gsn_server** out);
+/* Builds twiddle and coset tables for every (field, size) in the range up
+ * front, so first requests do not pay for table generation. */
+int gsn_server_warmup(gsn_server* s, int field, uint32_t log_n_min, uint32_t log_n_max);
+/* Enqueue a request (returns at once); *id identifies it. */
+int gsn_server_submit(gsn_server* s, const gsn_request* req, uint64_t* id);
+/* Block until request `id` is done (GSN_ERR_TIMEOUT after timeout_s seconds);
+ * latency_s (nullable) receives submit-to-done seconds. */
+int gsn_server_wait(gsn_server* s, uint64_t id, double timeout_s, double* latency_s);
+/* Copy a resident result to host memory and release its device memory. */
+int gsn_server_fetch(gsn_server* s, uint64_t id, uint32_t* host_out);
+/* Release a resident result without copying it. */
+int gsn_server_release(gsn_server* s, uint64_t id);
+int gsn_server_get_stats(gsn_server* s, gsn_server_stats* st);
+int gsn_server_destroy(gsn_server* s);
+
+typedef struct gsn_trace_entry {
+  double arrival_s; /* offset from the start of the trace */
+  gsn_request req;
+} gsn_trace_entry;
+
+/* Replays a trace: a feeder thread submits each entry at its arrival time;
+ * latencies_out[i] = done time - scheduled arrival of entry i (seconds);
+ * *makespan_s = first arrival to last completion. */
+int gsn_server_run_trace(gsn_server* s, const gsn_trace_entry* trace, size_t n, double* latencies_out,
+                         double* makespan_s);
+
 /* Fill device memory with uniform elements of [0, p): element i, limb j are
  * drawn from splitmix64 of (seed, i, attempt) with rejection sampling;
  * deterministic for a given seed. */

@@ -1,0 +1,93 @@
+"""Batched persistent launch: bit-exact against the plain per-call path and
+the oracle, with and without CUDA-graph capture."""
+import numpy as np
+import pytest
+
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+def _make_jobs(g, torch, f, sizes, dirs, seed):
+    from gpusnarks_gb300.batch import fill_random
+    total = sum(1 << k for k in sizes)
+    pool = torch.empty(total * f.limbs, dtype=torch.int32, device="cuda")
+    fill_random(f, pool, seed)
+    views, jobs, off = [], [], 0
+    for k, d in zip(sizes, dirs):
+        v = pool[off * f.limbs:(off + (1 << k)) * f.limbs]
+        views.append(v)
+        jobs.append((v.data_ptr(), k, d, None, None))
+        off += 1 << k
+    return pool, views, jobs
+
+
+@pytest.mark.parametrize("fname,lo,hi,count", [("bls12_381_fr", 2, 14, 48), ("mnt4753_fr", 1, 11, 24),
+                                               ("p32", 3, 16, 40)])
+@pytest.mark.parametrize("graph", [True, False])
+def test_batch_matches_per_call(gsn, cuda_device, fname, lo, hi, count, graph):
+    import torch
+    from gpusnarks_gb300.batch import Batch
+    f = gsn.FIELDS[fname]
+    rng = np.random.default_rng(count + lo)
+    sizes = [int(k) for k in rng.integers(lo, hi + 1, size=count)]
+    dirs = [int(d) for d in rng.choice([0, 1, 2, 3], size=count)]
+    pool, views, jobs = _make_jobs(gsn, torch, f, sizes, dirs, 0x5EED0400 + count)
+    ref = [v.clone() for v in views]
+    for r, k, d in zip(ref, sizes, dirs):
+        gsn.ntt(f, r, direction=d)
+    b = Batch(f, jobs, graph=graph)
+    b.launch()
+    torch.cuda.synchronize()
+    b.status()
+    for v, r, k in zip(views, ref, sizes):
+        assert torch.equal(v, r), k
+    # a second launch (graph replay) applies the transforms again
+    again = [v.clone() for v in views]
+    for r, d in zip(again, dirs):
+        gsn.ntt(f, r, direction=d)
+    b.launch()
+    torch.cuda.synchronize()
+    b.status()
+    for v, r in zip(views, again):
+        assert torch.equal(v, r)
+    info = b.info()
+    assert info["jobs"] == count and info["elements"] == sum(1 << k for k in sizes)
+    b.close()
+
+
+def test_batch_matches_oracle(gsn, cuda_device):
+    import torch
+    from gpusnarks_gb300.batch import Batch
+    f = gsn.BLS12_381
+    sizes = [9, 3, 12, 0, 1, 10]
+    pool, views, jobs = _make_jobs(gsn, torch, f, sizes, [0] * len(sizes), 0x5EED0444)
+    host = [gsn.to_host(v).reshape(-1, f.limbs).copy() for v in views]
+    b = Batch(f, jobs)
+    b.launch()
+    torch.cuda.synchronize()
+    for v, x in zip(views, host):
+        assert np.array_equal(gsn.to_host(v).reshape(x.shape), O.ntt(1, x).reshape(x.shape))
+    b.close()
+
+
+def test_device_random_matches_host_replica(gsn, cuda_device):
+    import torch
+    from gpusnarks_gb300.batch import fill_random
+    for f in (gsn.P32, gsn.BLS12_381, gsn.MNT4_753):
+        d = torch.empty(1000 * f.limbs, dtype=torch.int32, device="cuda")
+        fill_random(f, d, 1234)
+        assert np.array_equal(gsn.to_host(d).reshape(f.shape(1000)), f.device_random(1000, 1234))
+
+
+def test_batch_rejects_bad_jobs(gsn, cuda_device):
+    import torch
+    from gpusnarks_gb300.batch import Batch
+    f = gsn.BLS12_381
+    d = torch.empty(64 * f.limbs, dtype=torch.int32, device="cuda")
+    with pytest.raises(gsn.GsnError, match="ARG"):
+        Batch(f, [(d.data_ptr() + 4, 4, 0, None, None)])
+    with pytest.raises(gsn.GsnError, match="SIZE"):
+        Batch(f, [(d.data_ptr(), 40, 0, None, None)])
+    with pytest.raises(gsn.GsnError, match="OMEGA"):
+        Batch(f, [(d.data_ptr(), 4, 0, 2, None)])

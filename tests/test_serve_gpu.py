@@ -1,0 +1,100 @@
+"""Serving: every result equals the plain path, alone and in a mix, under an
+HBM budget that forces requests to wait for memory."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _plain(g, f, x, d):
+    t = g.to_device(x)
+    g.ntt(f, t, direction=d)
+    return g.to_host(t).reshape(x.shape)
+
+
+def _requests(g, count, seed, lo=5, hi=12):
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        f = (g.BLS12_381, g.MNT4_753)[int(rng.integers(0, 2))]
+        k = int(rng.integers(lo, hi + 1))
+        d = int(rng.integers(0, 3))
+        x = f.random_array(1 << k, seed=seed * 1000 + i)
+        out.append((f, k, d, x))
+    return out
+
+
+def test_results_match_plain_path_alone_and_in_mix(gsn, cuda_device):
+    from gpusnarks_gb300.serve import Server
+    reqs = _requests(gsn, 40, 7)
+    want = [_plain(gsn, f, x, d) for f, k, d, x in reqs]
+    srv = Server(1 << 30, max_inflight=3)
+    try:
+        # alone: one request at a time
+        alone = []
+        for f, k, d, x in reqs[:6]:
+            out = np.empty_like(x)
+            rid = srv.submit(f, x, d, host_out=out)
+            srv.wait(rid)
+            srv.release(rid)
+            alone.append(out)
+        # in the mix: everything at once
+        outs = [np.empty_like(x) for _, _, _, x in reqs]
+        ids = [srv.submit(f, x, d, host_out=o) for (f, k, d, x), o in zip(reqs, outs)]
+        for rid in ids:
+            srv.wait(rid)
+            srv.release(rid)
+        for o, w in zip(outs, want):
+            assert np.array_equal(o, w)
+        for a, o in zip(alone, outs[:6]):
+            assert np.array_equal(a, o)
+        st = srv.stats()
+        assert st["completed"] == 46 and st["failed"] == 0
+    finally:
+        srv.close()
+
+
+def test_budget_admission_and_resident_results(gsn, cuda_device):
+    from gpusnarks_gb300.serve import Server
+    f = gsn.MNT4_753
+    xs = [f.random_array(1 << 12, seed=300 + i) for i in range(12)]
+    want = [_plain(gsn, f, x, 0) for x in xs]
+    per = (1 << 12) * 96 * 2
+    srv = Server(3 * per + 4096, max_inflight=2)  # about three requests fit at once
+    try:
+        ids = [srv.submit(f, x, 0) for x in xs]  # results stay resident
+        for rid, w, x in zip(ids, want, xs):
+            srv.wait(rid)
+            out = np.empty_like(x)
+            srv.fetch(rid, out)
+            srv.release(rid)
+            assert np.array_equal(out, w)
+        assert srv.stats()["device_bytes_peak"] <= 3 * per + 4096
+        with pytest.raises(gsn.GsnError, match="NOMEM"):
+            srv.submit(f, f.random_array(1 << 14, seed=1), 0)
+    finally:
+        srv.close()
+
+
+def test_run_trace_small(gsn, cuda_device):
+    from gpusnarks_gb300.serve import Request, Server, TraceEntry, poisson_trace
+    trace = poisson_trace(30, 2000.0, 5, lo=6, hi=11)
+    ins, outs, entries, want = [], [], [], []
+    for i, (t, fid, k, d) in enumerate(trace):
+        f = gsn.BY_ID[fid]
+        x = f.random_array(1 << k, seed=900 + i)
+        o = np.empty_like(x)
+        ins.append(x)
+        outs.append(o)
+        want.append(_plain(gsn, f, x, d))
+        entries.append(TraceEntry(t, Request(fid, k, d, None, x.ctypes.data, o.ctypes.data)))
+    srv = Server(1 << 30, max_inflight=4)
+    try:
+        srv.warmup(1, 6, 11)
+        srv.warmup(2, 6, 11)
+        lat, makespan = srv.run_trace(entries)
+    finally:
+        srv.close()
+    assert (lat > 0).all() and makespan > 0
+    for o, w in zip(outs, want):
+        assert np.array_equal(o, w)
