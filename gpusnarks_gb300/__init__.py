@@ -121,6 +121,31 @@ def pointwise_mul(field, a, b, *, stream=None):
     return a
 
 
+def autotune(field, lo: int, hi: int, reps: int = 5) -> None:
+    """Time candidate plans for every log n in [lo, hi] and keep the fastest."""
+    check(load().gsn_autotune(field_of(field).fid, lo, hi, reps))
+
+
+def save_tuning(path) -> None:
+    check(load().gsn_tuning_save(str(path).encode()))
+
+
+def load_tuning(path) -> None:
+    check(load().gsn_tuning_load(str(path).encode()))
+
+
+def clear_tuning() -> None:
+    check(load().gsn_tuning_clear())
+
+
+def plan(field, log_n: int) -> dict:
+    """The plan (passes, radices, tile widths, threads, kernel) a transform would use."""
+    import json
+    buf = ctypes.create_string_buffer(1024)
+    check(load().gsn_plan_describe(field_of(field).fid, log_n, buf, len(buf)))
+    return json.loads(buf.value.decode())
+
+
 def launch_count() -> int:
     return int(load().gsn_kernel_launch_count())
 

@@ -50,6 +50,8 @@ _SIGNATURES = [
     ("gsn_kernel_launch_count", ctypes.c_uint64, []),
     ("gsn_microbench_imad", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    ("gsn_microbench_mont", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.POINTER(ctypes.c_double)]),
     ("gsn_batch_create", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_void_p)]),
     ("gsn_batch_launch", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),
@@ -61,7 +63,14 @@ _SIGNATURES = [
     ("gsn_batch_destroy", ctypes.c_int, [ctypes.c_void_p]),
     ("gsn_fill_random", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
                                        ctypes.c_void_p]),
+    ("gsn_autotune", ctypes.c_int, [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]),
+    ("gsn_tuning_save", ctypes.c_int, [ctypes.c_char_p]),
+    ("gsn_tuning_load", ctypes.c_int, [ctypes.c_char_p]),
+    ("gsn_tuning_clear", ctypes.c_int, []),
+    ("gsn_plan_describe", ctypes.c_int, [ctypes.c_int, ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t]),
 ]
+
+TUNING_FILE = pathlib.Path(__file__).resolve().parent / "tuning" / "gb300.json"
 
 
 class BatchJob(ctypes.Structure):
@@ -93,6 +102,8 @@ def load(build_if_missing: bool = False) -> ctypes.CDLL:
         fn.restype = res
         fn.argtypes = args
     _lib = lib
+    if TUNING_FILE.exists():  # plans measured on GB300 by gsn_autotune
+        lib.gsn_tuning_load(str(TUNING_FILE).encode())
     return lib
 
 

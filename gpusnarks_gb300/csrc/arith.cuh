@@ -170,7 +170,7 @@ __device__ __forceinline__ void cios_reduce_step(uint32_t (&t)[P::N + 2]) {
 // r = a * b * R^-1 mod p (CIOS, Koc-Acar-Kaliski), lo and hi partial
 // products in two carry chains per row.  Inputs canonical; output canonical.
 template <class P>
-__device__ __forceinline__ void fe_mul(Fe<P>& r, const Fe<P>& a, const Fe<P>& b) {
+__device__ __forceinline__ void fe_mul_rows(Fe<P>& r, const Fe<P>& a, const Fe<P>& b) {
   constexpr int N = P::N;
   if constexpr (N == 1) {
     r.l[0] = mul1<P>(a.l[0], b.l[0]);
@@ -209,6 +209,107 @@ __device__ __forceinline__ void fe_mul(Fe<P>& r, const Fe<P>& a, const Fe<P>& b)
     ptx::subc(mask, t[N], 0u);  // 0xFFFFFFFF iff t < p
 #pragma unroll
     for (int j = 0; j < N; ++j) r.l[j] = (t[j] & mask) | (d[j] & ~mask);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Even/odd-accumulator CIOS.  Same result as fe_mul_rows, different schedule:
+// every carry chain adds whole 64-bit products a_j*b into a non-overlapping
+// pair of accumulator words (mad.lo.cc then madc.hi.cc on the same operands,
+// into consecutive words), so each pair can issue as one wide multiply-add.
+// Even-indexed limbs accumulate into E, odd-indexed limbs into O one word
+// higher: T = E + 2^32 O.  After the reduction row E_0 is zero and
+// T / 2^32 = (O + E_1) + 2^32 (E_2 .. E_N), so the accumulators swap roles
+// with one add chain per row.
+// ---------------------------------------------------------------------------
+
+// acc[0..N] += sum_k x[2k + off] * y * 2^(64 k)
+template <int N>
+__device__ __forceinline__ void pair_chain(uint32_t (&acc)[N + 1], const uint32_t* x, int off, uint32_t y) {
+  ptx::mad_lo_cc(acc[0], x[off], y, acc[0]);
+  ptx::madc_hi_cc(acc[1], x[off], y, acc[1]);
+#pragma unroll
+  for (int k = 1; k < N / 2; ++k) {
+    ptx::madc_lo_cc(acc[2 * k], x[2 * k + off], y, acc[2 * k]);
+    ptx::madc_hi_cc(acc[2 * k + 1], x[2 * k + off], y, acc[2 * k + 1]);
+  }
+  ptx::addc(acc[N], acc[N], 0u);
+}
+
+// Same on the modulus limbs (compile-time constants).
+template <class P>
+__device__ __forceinline__ void pair_chain_mod(uint32_t (&acc)[P::N + 1], int off, uint32_t y) {
+  constexpr int N = P::N;
+  ptx::mad_lo_cc(acc[0], P::mod(off), y, acc[0]);
+  ptx::madc_hi_cc(acc[1], P::mod(off), y, acc[1]);
+#pragma unroll
+  for (int k = 1; k < N / 2; ++k) {
+    ptx::madc_lo_cc(acc[2 * k], P::mod(2 * k + off), y, acc[2 * k]);
+    ptx::madc_hi_cc(acc[2 * k + 1], P::mod(2 * k + off), y, acc[2 * k + 1]);
+  }
+  ptx::addc(acc[N], acc[N], 0u);
+}
+
+// r = a * b * R^-1 mod p, canonical in and out.  N even.
+template <class P>
+__device__ __forceinline__ void fe_mul_eo(Fe<P>& r, const Fe<P>& a, const Fe<P>& b) {
+  constexpr int N = P::N;
+  static_assert(N % 2 == 0, "even/odd schedule needs an even limb count");
+  uint32_t E[N + 1], O[N + 1];
+#pragma unroll
+  for (int j = 0; j <= N; ++j) E[j] = O[j] = 0u;
+#pragma unroll
+  for (int i = 0; i < N; ++i) {
+    pair_chain<N>(E, a.l, 0, b.l[i]);
+    pair_chain<N>(O, a.l, 1, b.l[i]);
+    const uint32_t m = E[0] * P::PINV;
+    pair_chain_mod<P>(E, 0, m);
+    pair_chain_mod<P>(O, 1, m);
+    // E <- O + E_1, O <- E_2..E_N (register renaming once unrolled)
+    uint32_t e1 = E[1];
+#pragma unroll
+    for (int j = 0; j <= N - 2; ++j) E[j] = E[j + 2];  // stash E_2.. (becomes O)
+    uint32_t Onew[N + 1];
+#pragma unroll
+    for (int j = 0; j <= N - 2; ++j) Onew[j] = E[j];
+    Onew[N - 1] = 0u;
+    Onew[N] = 0u;
+    ptx::add_cc(E[0], O[0], e1);
+#pragma unroll
+    for (int j = 1; j < N; ++j) ptx::addc_cc(E[j], O[j], 0u);
+    ptx::addc(E[N], O[N], 0u);
+#pragma unroll
+    for (int j = 0; j <= N; ++j) O[j] = Onew[j];
+  }
+  // t = E + 2^32 O  (< 2p), then one conditional subtraction
+  uint32_t t[N + 1];
+  t[0] = E[0];
+  ptx::add_cc(t[1], E[1], O[0]);
+#pragma unroll
+  for (int j = 2; j < N; ++j) ptx::addc_cc(t[j], E[j], O[j - 1]);
+  ptx::addc(t[N], E[N], O[N - 1]);
+  uint32_t d[N], mask;
+  ptx::sub_cc(d[0], t[0], P::mod(0));
+#pragma unroll
+  for (int j = 1; j < N; ++j) ptx::subc_cc(d[j], t[j], P::mod(j));
+  ptx::subc(mask, t[N], 0u);
+#pragma unroll
+  for (int j = 0; j < N; ++j) r.l[j] = (t[j] & mask) | (d[j] & ~mask);
+}
+
+// Montgomery product used by the kernels.  kMontSchedule selects the
+// multi-limb schedule: 1 = even/odd accumulators (default), 0 = row chains.
+#ifndef GSN_MONT_SCHEDULE
+#define GSN_MONT_SCHEDULE 1
+#endif
+template <class P, int S = GSN_MONT_SCHEDULE>
+__device__ __forceinline__ void fe_mul(Fe<P>& r, const Fe<P>& a, const Fe<P>& b) {
+  if constexpr (P::N == 1) {
+    r.l[0] = mul1<P>(a.l[0], b.l[0]);
+  } else if constexpr (S == 1 && P::N % 2 == 0) {
+    fe_mul_eo<P>(r, a, b);
+  } else {
+    fe_mul_rows<P>(r, a, b);
   }
 }
 

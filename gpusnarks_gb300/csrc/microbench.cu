@@ -14,6 +14,7 @@
 #include <cstdint>
 #include <vector>
 
+#include "arith.cuh"
 #include "gpusnarks_gb300.h"
 #include "runtime.h"
 
@@ -73,9 +74,75 @@ __global__ void imad_chain_kernel(uint32_t* sink, int iters, uint32_t x, uint32_
   }
 }
 
+// Throughput of the field Montgomery product itself: every thread runs two
+// independent chains x <- x * y.  S selects the multi-limb schedule.
+template <class P, int S>
+__global__ void mont_chain_kernel(uint32_t* sink, int iters) {
+  Fe<P> x1, x2, y;
+#pragma unroll
+  for (int j = 0; j < P::N; ++j) {
+    x1.l[j] = (threadIdx.x + 1) * 0x9E3779B9u + j;
+    x2.l[j] = (blockIdx.x + 7) * 0x85EBCA6Bu + 3 * j;
+    y.l[j] = 0xC2B2AE35u * (j + 11) + (blockIdx.x ^ threadIdx.x);  // runtime values, like a twiddle
+  }
+  x1.l[P::N - 1] &= 0xFFFFu;  // below every modulus here
+  x2.l[P::N - 1] &= 0xFFFFu;
+  y.l[P::N - 1] &= 0xFFFFu;
+  for (int it = 0; it < iters; ++it) {
+    fe_mul<P, S>(x1, x1, y);
+    fe_mul<P, S>(x2, x2, y);
+  }
+  uint32_t acc = 0;
+#pragma unroll
+  for (int j = 0; j < P::N; ++j) acc ^= x1.l[j] ^ (x2.l[j] * (j + 1));
+  sink[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
+template <class P, int S>
+static int run_mont_bench(int iters, double* muls_per_s) {
+  int dev = 0, sms = 0, per_sm = 0;
+  GSN_CUDA(cudaGetDevice(&dev));
+  GSN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int block = 128;
+  GSN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mont_chain_kernel<P, S>, block, 0));
+  const int grid = sms * std::max(per_sm, 1);
+  uint32_t* sink = nullptr;
+  int rc = dev_alloc((void**)&sink, (size_t)grid * block * sizeof(uint32_t));
+  if (rc) return rc;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  mont_chain_kernel<P, S><<<grid, block>>>(sink, iters / 8 + 1);
+  cudaEventRecord(e0);
+  mont_chain_kernel<P, S><<<grid, block>>>(sink, iters);
+  cudaEventRecord(e1);
+  cudaError_t err = cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  dev_free(sink);
+  count_launches(2);
+  if (err != cudaSuccess) return cuda_fail(err, "Montgomery microbenchmark");
+  *muls_per_s = 2.0 * grid * block * (double)iters / (ms * 1e-3);
+  return GSN_OK;
+}
+
 }  // namespace gsn
 
 using namespace gsn;
+
+extern "C" int gsn_microbench_mont(int field, int schedule, int iters, double* muls_per_s) {
+  if (iters <= 0 || !muls_per_s || (schedule != 0 && schedule != 1))
+    return set_error(GSN_ERR_ARG, "bad microbenchmark arguments");
+  switch (field * 2 + schedule) {
+    case GSN_BLS12_381_FR * 2 + 0: return run_mont_bench<FieldBLS12_381, 0>(iters, muls_per_s);
+    case GSN_BLS12_381_FR * 2 + 1: return run_mont_bench<FieldBLS12_381, 1>(iters, muls_per_s);
+    case GSN_MNT4753_FR * 2 + 0: return run_mont_bench<FieldMNT4_753, 0>(iters, muls_per_s);
+    case GSN_MNT4753_FR * 2 + 1: return run_mont_bench<FieldMNT4_753, 1>(iters, muls_per_s);
+    default: return set_error(GSN_ERR_FIELD, "Montgomery microbenchmark covers the multi-limb fields");
+  }
+}
 
 extern "C" int gsn_microbench_imad(int iters, double* mads_per_s, double* mads_per_clk_sm, double* sm_mhz) {
   if (iters <= 0 || !mads_per_s) return set_error(GSN_ERR_ARG, "bad microbenchmark arguments");

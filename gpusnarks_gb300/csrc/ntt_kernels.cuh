@@ -17,6 +17,12 @@
 
 namespace gsn {
 
+// Dynamic shared memory above this is requested explicitly with
+// cudaFuncAttributeMaxDynamicSharedMemorySize.  It is below the 48 KB default
+// so that kernels with a little static shared memory (the batch kernel keeps
+// its ticket and pass arguments there) never exceed the default limit.
+constexpr size_t kDefaultSmemOptIn = 32 * 1024;
+
 __device__ __forceinline__ uint32_t bitrev_bits(uint32_t x, int bits) {
   return bits == 0 ? 0u : (__brev(x) >> (32 - bits));
 }
@@ -83,93 +89,95 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
     obase = k0 + (rest_offset(rest, A.npass, A.radix_log) << lo0);
   }
 
-  Fe<P> pre_c;
-  if (A.first && A.has_pre_const) {
-#pragma unroll
-    for (int w = 0; w < N; ++w) pre_c.l[w] = A.pre_const[w];
-  }
+  // global position of tile element (k, jj) in the source array
+  auto src_pos = [&](int k, int jj) -> uint64_t {
+    return !A.last ? base + ((uint64_t)k << A.log_inner) + jj
+                   : ((rowpre + ((uint64_t)jj << (A.log_outer - lo0))) << lr) + k;
+  };
 
-  // --- load ----------------------------------------------------------------
+  // --- load (no arithmetic) ------------------------------------------------
   for (int e = tid; e < R * J; e += nthr) {
     int k, jj;
-    uint64_t gpos;
     if (!A.last) {
       k = e >> lj;
       jj = e & (J - 1);
-      gpos = base + ((uint64_t)k << A.log_inner) + jj;
     } else {
-      jj = e >> lr;
+      jj = e >> lr;  // input rows are contiguous on the last pass
       k = e & (R - 1);
-      gpos = ((rowpre + ((uint64_t)jj << (A.log_outer - lo0))) << lr) + k;
     }
     Fe<P> x;
-    fe_load_cg<P>(x, A.src + gpos * N);
-    if (A.first) {
-      if (A.pre_table) {
-        Fe<P> s;
-        fe_load<P>(s, A.pre_table + gpos * N);
-        fe_mul<P>(x, x, s);
-      }
-      if (A.has_pre_const) fe_mul<P>(x, x, pre_c);
-    }
-    fe_store<P>(sm + ((uint64_t)((k << lj) + jj)) * N, x);
+    fe_load_cg<P>(x, A.src + src_pos(k, jj) * N);
+    fe_store<P>(sm + ((k << lj) + jj) * N, x);
   }
   __syncthreads();
 
-  // --- radix-2 DIF stages (natural in, bit-reversed out within the tile) ---
-  for (int s = 0; s < lr; ++s) {
-    const int log_half = lr - 1 - s;
-    for (int b = tid; b < (R >> 1) * J; b += nthr) {
-      const int jj = b & (J - 1);
-      const int bb = b >> lj;
-      const int i = bb & ((1 << log_half) - 1);
-      const int g = bb >> log_half;
-      const int u = (g << (log_half + 1)) + i;
-      const int v = u + (1 << log_half);
-      Fe<P> x, y, sum, dif;
-      fe_load<P>(x, sm + ((u << lj) + jj) * N);
-      fe_load<P>(y, sm + ((v << lj) + jj) * N);
-      fe_add<P>(sum, x, y);
-      fe_sub<P>(dif, x, y);
-      if (i != 0) {
-        Fe<P> w;
-        const uint64_t e = ((uint64_t)i << s) << (A.log_n - lr);
-        tw_load<P>(w, A.tw, tw_index(A.tw_log, A.log_n, A.inverse, e));
-        fe_mul<P>(dif, dif, w);
+  // --- phases; every multiplication goes through the single fe_mul below, so
+  // the fully unrolled product exists once in the instruction stream --------
+  //   ph = -1        pre-scale (first pass: coset powers or n^-1)
+  //   ph = 0..lr-1   radix-2 DIF stage ph (natural in, bit-reversed out)
+  //   ph = lr        four-step twiddle (non-last) or post table (last), store
+  const bool pre = A.first && (A.pre_table || A.has_pre_const);
+  for (int ph = pre ? -1 : 0; ph <= lr; ++ph) {
+    const bool stage = ph >= 0 && ph < lr;
+    const int count = stage ? (R >> 1) * J : R * J;
+    for (int b = tid; b < count; b += nthr) {
+      Fe<P> x, w;
+      bool mul = false;
+      uint32_t* out;
+      if (ph < 0) {
+        const int k = b >> lj, jj = b & (J - 1);
+        out = sm + ((k << lj) + jj) * N;
+        fe_load<P>(x, out);
+        if (A.pre_table) {
+          fe_load<P>(w, A.pre_table + src_pos(k, jj) * N);
+        } else {
+#pragma unroll
+          for (int l = 0; l < N; ++l) w.l[l] = A.pre_const[l];
+        }
+        mul = true;
+      } else if (stage) {
+        const int log_half = lr - 1 - ph;
+        const int jj = b & (J - 1);
+        const int bb = b >> lj;
+        const int i = bb & ((1 << log_half) - 1);
+        const int u = ((bb >> log_half) << (log_half + 1)) + i;
+        const int v = u + (1 << log_half);
+        Fe<P> y, sum;
+        fe_load<P>(x, sm + ((u << lj) + jj) * N);
+        fe_load<P>(y, sm + ((v << lj) + jj) * N);
+        fe_add<P>(sum, x, y);
+        fe_sub<P>(x, x, y);
+        fe_store<P>(sm + ((u << lj) + jj) * N, sum);
+        out = sm + ((v << lj) + jj) * N;
+        if (i != 0) {
+          const uint64_t e = ((uint64_t)i << ph) << (A.log_n - lr);
+          tw_load<P>(w, A.tw, tw_index(A.tw_log, A.log_n, A.inverse, e));
+          mul = true;
+        }
+      } else {
+        const int k = b >> lj, jj = b & (J - 1);
+        fe_load<P>(x, sm + ((bitrev_bits((uint32_t)k, lr) << lj) + jj) * N);
+        if (!A.last) {
+          const uint64_t ex = ((jbase + jj) * (uint64_t)k) << A.log_outer;
+          out = A.dst + (base + ((uint64_t)k << A.log_inner) + jj) * N;
+          if (ex != 0) {
+            tw_load<P>(w, A.tw, tw_index(A.tw_log, A.log_n, A.inverse, ex));
+            mul = true;
+          }
+        } else {
+          const uint64_t opos = obase + jj + ((uint64_t)k << A.log_outer);
+          out = A.dst + opos * N;
+          if (A.post_table) {
+            fe_load<P>(w, A.post_table + opos * N);
+            mul = true;
+          }
+        }
       }
-      fe_store<P>(sm + ((u << lj) + jj) * N, sum);
-      fe_store<P>(sm + ((v << lj) + jj) * N, dif);
+      if (mul) fe_mul<P>(x, x, w);
+      fe_store<P>(out, x);
     }
     __syncthreads();
   }
-
-  // --- twiddle and store ---------------------------------------------------
-  for (int e = tid; e < R * J; e += nthr) {
-    const int k = e >> lj;
-    const int jj = e & (J - 1);
-    const uint32_t q = bitrev_bits((uint32_t)k, lr);
-    Fe<P> x;
-    fe_load<P>(x, sm + ((q << lj) + jj) * N);
-    if (!A.last) {
-      const uint64_t jp = jbase + jj;
-      const uint64_t ex = (jp * (uint64_t)k) << A.log_outer;
-      if (ex != 0) {
-        Fe<P> w;
-        tw_load<P>(w, A.tw, tw_index(A.tw_log, A.log_n, A.inverse, ex));
-        fe_mul<P>(x, x, w);
-      }
-      fe_store<P>(A.dst + (base + ((uint64_t)k << A.log_inner) + jj) * N, x);
-    } else {
-      const uint64_t opos = obase + jj + ((uint64_t)k << A.log_outer);
-      if (A.post_table) {
-        Fe<P> s;
-        fe_load<P>(s, A.post_table + opos * N);
-        fe_mul<P>(x, x, s);
-      }
-      fe_store<P>(A.dst + opos * N, x);
-    }
-  }
-  __syncthreads();
 }
 
 template <class P>
@@ -359,7 +367,7 @@ struct Kernels {
   static cudaError_t pass(const PassArgs& A, int block, cudaStream_t s) {
     const size_t smem = ((size_t)1 << (A.log_r + A.log_j)) * P::N * sizeof(uint32_t);
     auto k = ntt_pass_kernel<P>;
-    if (smem > 48 * 1024) {
+    if (smem > kDefaultSmemOptIn) {
       cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
     }
@@ -379,7 +387,7 @@ struct Kernels {
                            uint32_t* counters_dev, uint32_t* status_dev, int grid, int block, size_t smem,
                            cudaStream_t s) {
     auto k = batch_kernel<P>;
-    if (smem > 48 * 1024) {
+    if (smem > kDefaultSmemOptIn) {
       cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
     }
@@ -388,7 +396,7 @@ struct Kernels {
   }
   static int batch_occupancy(int block, size_t smem) {
     auto k = batch_kernel<P>;
-    if (smem > 48 * 1024) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (smem > kDefaultSmemOptIn) cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, block, smem) != cudaSuccess) return 0;
     return nb;

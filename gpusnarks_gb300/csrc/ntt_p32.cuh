@@ -245,7 +245,7 @@ struct P32Kernels {
   static cudaError_t launch_one(const P32Args& A, int block, int grid_cap, cudaStream_t s) {
     const size_t smem = ((size_t)1 << (A.log_r + A.log_j)) * sizeof(uint32_t);
     auto k = ntt_p32_kernel<ET, LCG>;
-    if (smem > 48 * 1024) {
+    if (smem > kDefaultSmemOptIn) {
       cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
     }

@@ -133,6 +133,19 @@ int gsn_batch_status(gsn_batch* b);
 int gsn_batch_info(gsn_batch* b, uint64_t* njobs, uint64_t* nwork, uint64_t* elements, uint64_t* device_bytes);
 int gsn_batch_destroy(gsn_batch* b);
 
+/* ---- autotuning (no reference counterpart: the reference hard-codes 1024
+ * chunks of 64 points, cuda/fft_kernel.cu:56-59) --------------------------- */
+
+/* Times candidate plans (pass split, tile width, threads, kernel variant)
+ * for every log_n in [lo, hi] on the current device, `reps` timed runs each,
+ * and keeps the fastest for later transforms, batches and the server. */
+int gsn_autotune(int field, uint32_t log_n_lo, uint32_t log_n_hi, int reps);
+int gsn_tuning_save(const char* path); /* JSON */
+int gsn_tuning_load(const char* path);
+int gsn_tuning_clear(void);
+/* JSON description of the plan a transform of (field, log_n) would use. */
+int gsn_plan_describe(int field, uint32_t log_n, char* buf, size_t len);
+
 /* ---- serving (no reference counterpart) -----------------------------------
  * A request loop that admits forward / inverse / coset NTT jobs of mixed
  * fields and sizes under an HBM budget, keeps polynomials and twiddle tables
@@ -210,6 +223,9 @@ uint64_t gsn_kernel_launch_count(void);
  * Montgomery products use, on every SM at full occupancy.  Returns PTX
  * multiply-adds per second, per SM per clock, and the SM clock seen. */
 int gsn_microbench_imad(int iters, double* mads_per_s, double* mads_per_clk_sm, double* sm_mhz);
+/* Throughput (products per second, all SMs) of the multi-limb Montgomery
+ * product with schedule 0 (row chains) or 1 (even/odd accumulators). */
+int gsn_microbench_mont(int field, int schedule, int iters, double* muls_per_s);
 
 #ifdef __cplusplus
 }
