@@ -106,6 +106,7 @@ struct Req {
   bool has_data = false, has_scratch = false;
   State st = kPending;
   int rc = GSN_OK;
+  std::string err;  // message of a failure, captured on the scheduler thread
   cudaEvent_t ev = nullptr;
   Clock::time_point t_submit, t_done;
 };
@@ -169,6 +170,7 @@ void free_mem(gsn_server* S, Req& q, bool data_too) {
 void finish(gsn_server* S, Req& q, State st, int rc) {
   q.st = st;
   q.rc = rc;
+  if (st == kFailed) q.err = gsn_last_error();
   q.t_done = Clock::now();
   if (st == kFailed) {
     ++S->failed;
@@ -478,7 +480,8 @@ int gsn_server_wait(gsn_server* S, uint64_t id, double timeout_s, double* latenc
     Req& q = S->reqs[id];
     if (q.st == kDone || q.st == kResident || q.st == kFailed) {
       if (latency_s) *latency_s = seconds(q.t_done - q.t_submit);
-      if (q.st == kFailed) return set_error(q.rc, "request %llu failed", (unsigned long long)id);
+      if (q.st == kFailed)
+        return set_error(q.rc, "request %llu failed: %s", (unsigned long long)id, q.err.c_str());
       return GSN_OK;
     }
     if (S->done_cv.wait_until(lk, deadline) == std::cv_status::timeout && Clock::now() >= deadline)
@@ -570,15 +573,22 @@ int gsn_server_run_trace(gsn_server* S, const gsn_trace_entry* trace, size_t n, 
   });
   feeder.join();
   int first_err = GSN_OK;
+  std::string first_msg;
   Clock::time_point last = t0;
   for (size_t i = 0; i < n; ++i) {
     if (rcs[i]) {
-      if (!first_err) first_err = rcs[i];
+      if (!first_err) {
+        first_err = rcs[i];
+        first_msg = "submit of entry " + std::to_string(i) + " failed";
+      }
       if (latencies_out) latencies_out[i] = -1;
       continue;
     }
     int rc = gsn_server_wait(S, ids[i], 600.0, nullptr);
-    if (rc && !first_err) first_err = rc;
+    if (rc && !first_err) {
+      first_err = rc;
+      first_msg = gsn_last_error();
+    }
     std::lock_guard<std::mutex> g(S->mu);
     Req& q = S->reqs[ids[i]];
     const Clock::time_point arr = t0 + std::chrono::duration_cast<Clock::duration>(
@@ -595,7 +605,7 @@ int gsn_server_run_trace(gsn_server* S, const gsn_trace_entry* trace, size_t n, 
     }
   for (size_t i = 0; i < n; ++i)
     if (ids[i]) gsn_server_release(S, ids[i]);
-  if (first_err) return set_error(first_err, "trace finished with errors (first: %d)", first_err);
+  if (first_err) return set_error(first_err, "trace finished with errors; first: %s", first_msg.c_str());
   return GSN_OK;
 }
 
