@@ -121,9 +121,11 @@ def pointwise_mul(field, a, b, *, stream=None):
     return a
 
 
-def autotune(field, lo: int, hi: int, reps: int = 5) -> None:
-    """Time candidate plans for every log n in [lo, hi] and keep the fastest."""
-    check(load().gsn_autotune(field_of(field).fid, lo, hi, reps))
+def autotune(field, lo: int, hi: int, reps: int = 5, *, batched: bool = False) -> None:
+    """Time candidate plans for every log n in [lo, hi] and keep the fastest
+    (for single transforms, or for the persistent batched kernel)."""
+    fn = load().gsn_autotune_batch if batched else load().gsn_autotune
+    check(fn(field_of(field).fid, lo, hi, reps))
 
 
 def save_tuning(path) -> None:

@@ -61,9 +61,11 @@ _SIGNATURES = [
                                       ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
                                       ctypes.POINTER(ctypes.c_uint64)]),
     ("gsn_batch_destroy", ctypes.c_int, [ctypes.c_void_p]),
+    ("gsn_batch_selftest_wait", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32)]),
     ("gsn_fill_random", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
                                        ctypes.c_void_p]),
     ("gsn_autotune", ctypes.c_int, [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]),
+    ("gsn_autotune_batch", ctypes.c_int, [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]),
     ("gsn_tuning_save", ctypes.c_int, [ctypes.c_char_p]),
     ("gsn_tuning_load", ctypes.c_int, [ctypes.c_char_p]),
     ("gsn_tuning_clear", ctypes.c_int, []),

@@ -11,6 +11,8 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
+#include <tuple>
 #include <cstring>
 #include <fstream>
 #include <map>
@@ -84,9 +86,76 @@ int time_plan(const FieldOps& F, const Plan& plan, uint32_t* data, uint32_t* scr
   return rc;
 }
 
-std::string plan_json(int field, const Plan& p, float ms) {
+// Times `plan` inside the persistent batch kernel on enough equal jobs to
+// fill the GPU (total_elems elements in all).
+int time_batch_plan(const FieldOps& F, const Plan& plan, uint32_t* data, uint32_t* scratch, uint64_t total_elems,
+                    int reps, float* ms) {
+  const uint64_t n = (uint64_t)1 << plan.log_n;
+  const size_t njobs = (size_t)std::max<uint64_t>(1, total_elems / n);
+  std::vector<gsn_batch_job> jobs(njobs);
+  for (size_t i = 0; i < njobs; ++i) {
+    jobs[i].data = data + i * n * F.limbs;
+    jobs[i].log_n = (uint32_t)plan.log_n;
+    jobs[i].dir = GSN_FORWARD;
+    jobs[i].omega = nullptr;
+    jobs[i].shift = nullptr;
+  }
+  BatchPlan bp;
+  int rc = plan_batch(F, jobs.data(), njobs, &bp, &plan);
+  if (rc) return rc;
+  if (job_scratch_bytes(F, plan))
+    for (size_t i = 0; i < njobs; ++i) bp.jobs[i].scratch = scratch + i * n * F.limbs;
+  BatchJob* jobs_dev = nullptr;
+  uint64_t* work_dev = nullptr;
+  uint32_t *counters = nullptr, *status = nullptr;
+  const size_t cbytes = (1 + njobs * kMaxPasses) * sizeof(uint32_t);
+  rc = dev_alloc((void**)&jobs_dev, njobs * sizeof(BatchJob));
+  if (!rc) rc = dev_alloc((void**)&work_dev, bp.work.size() * sizeof(uint64_t));
+  if (!rc) rc = dev_alloc((void**)&counters, cbytes);
+  if (!rc) rc = dev_alloc((void**)&status, sizeof(uint32_t));
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  const int per_sm = rc ? 0 : F.batch_occupancy(bp.block, bp.smem);
+  if (!rc && per_sm < 1) rc = set_error(GSN_ERR_ARG, "batch candidate does not fit an SM");
+  cudaEvent_t a = nullptr, b = nullptr;
+  float best = 1e30f;
+  if (!rc) {
+    cudaMemcpy(jobs_dev, bp.jobs.data(), njobs * sizeof(BatchJob), cudaMemcpyHostToDevice);
+    cudaMemcpy(work_dev, bp.work.data(), bp.work.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    for (int i = 0; i < reps + 1 && !rc; ++i) {
+      cudaEventRecord(a);
+      cudaMemsetAsync(counters, 0, cbytes);
+      cudaMemsetAsync(status, 0, sizeof(uint32_t));
+      cudaError_t e = F.batch(jobs_dev, work_dev, bp.work.size(), counters, status, sms * per_sm, bp.block, bp.smem,
+                              nullptr, 0);
+      cudaEventRecord(b);
+      if (e == cudaSuccess) e = cudaEventSynchronize(b);
+      if (e != cudaSuccess) {
+        rc = cuda_fail(e, "batch candidate");
+        break;
+      }
+      float t = 0;
+      cudaEventElapsedTime(&t, a, b);
+      if (i > 0) best = std::min(best, t);  // the first run is a warm-up
+    }
+    count_launches((uint64_t)reps + 1);
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+  }
+  dev_free(jobs_dev);
+  dev_free(work_dev);
+  dev_free(counters);
+  dev_free(status);
+  *ms = best;
+  return rc;
+}
+
+std::string plan_json(int field, const Plan& p, float ms, int mode) {
   std::ostringstream o;
-  o << "{\"field\": " << field << ", \"log_n\": " << p.log_n << ", \"kernel\": " << p.kernel
+  o << "{\"field\": " << field << ", \"mode\": " << mode << ", \"log_n\": " << p.log_n << ", \"kernel\": " << p.kernel
     << ", \"e_log\": " << p.e_log << ", \"npass\": " << p.npass << ", \"radix_log\": [";
   for (int i = 0; i < kMaxPasses; ++i) o << (i ? ", " : "") << p.radix_log[i];
   o << "], \"log_j\": [";
@@ -97,7 +166,7 @@ std::string plan_json(int field, const Plan& p, float ms) {
   return o.str();
 }
 
-std::map<std::pair<int, int>, float> g_tuned_ms;
+std::map<std::tuple<int, int, int>, float> g_tuned_ms;  // (field, log_n, mode)
 
 // Minimal reader for the files plan_json writes: finds "key": value or
 // "key": [a, b, c, d] inside one object.
@@ -121,12 +190,16 @@ using namespace gsn;
 
 extern "C" {
 
-int gsn_autotune(int field, uint32_t lo, uint32_t hi, int reps) {
+static int autotune_impl(int field, uint32_t lo, uint32_t hi, int reps, int mode) {
   const FieldOps* F = field_ops(field);
   if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);
   if (hi < lo || (int)hi > std::min(F->max_log_n, F->two_adicity)) return set_error(GSN_ERR_SIZE, "bad range");
   if (reps < 1) reps = 5;
-  const size_t bytes = ((size_t)1 << hi) * F->limbs * sizeof(uint32_t);
+  const bool verbose = std::getenv("GSN_TUNE_VERBOSE") != nullptr;
+  // batch mode times GPU-filling sets of equal jobs of this many elements
+  const uint64_t batch_elems = (uint64_t)1 << (F->limbs == 1 ? 24 : (F->limbs == 8 ? 23 : 22));
+  const uint64_t elems = std::max<uint64_t>((uint64_t)1 << hi, mode ? batch_elems : 0);
+  const size_t bytes = elems * F->limbs * sizeof(uint32_t);
   uint32_t *data = nullptr, *scratch = nullptr;
   int rc = dev_alloc((void**)&data, bytes);
   if (!rc) rc = dev_alloc((void**)&scratch, bytes);
@@ -134,33 +207,47 @@ int gsn_autotune(int field, uint32_t lo, uint32_t hi, int reps) {
     dev_free(data);
     return rc;
   }
-  cudaError_t e = F->fill(data, (uint64_t)1 << hi, 0x5EED7E57ull, nullptr);
+  cudaError_t e = F->fill(data, elems, 0x5EED7E57ull, nullptr);
   if (e != cudaSuccess) rc = cuda_fail(e, "autotune fill");
   for (uint32_t k = lo; k <= hi && !rc; ++k) {
     Plan best;
     float best_ms = 1e30f;
+    int timed = 0, skipped = 0;
     for (const Plan& p : candidates(*F, (int)k)) {
+      if (mode == 1 && p.kernel != kKernelGeneric) continue;
       float ms = 0;
-      int r = time_plan(*F, p, data, scratch, reps, &ms);
+      int r = mode == 1 ? time_batch_plan(*F, p, data, scratch, batch_elems, reps, &ms)
+                        : time_plan(*F, p, data, scratch, reps, &ms);
       if (r) {
         // a candidate that cannot launch (resources) is skipped, not fatal
         cudaGetLastError();
+        ++skipped;
         continue;
       }
+      ++timed;
       if (ms < best_ms) {
         best_ms = ms;
         best = p;
       }
     }
+    if (verbose)
+      std::fprintf(stderr, "autotune field %d mode %d 2^%u: %d timed, %d skipped, best %.4f ms\n", field, mode, k,
+                   timed, skipped, best_ms);
     if (best_ms < 1e30f) {
-      set_tuned_plan(F->id, (int)k, best);
-      g_tuned_ms[{F->id, (int)k}] = best_ms;
+      set_tuned_plan(F->id, (int)k, best, mode);
+      g_tuned_ms[std::make_tuple(F->id, (int)k, mode)] = best_ms;
     }
   }
   cudaDeviceSynchronize();
   dev_free(data);
   dev_free(scratch);
   return rc;
+}
+
+int gsn_autotune(int field, uint32_t lo, uint32_t hi, int reps) { return autotune_impl(field, lo, hi, reps, 0); }
+
+int gsn_autotune_batch(int field, uint32_t lo, uint32_t hi, int reps) {
+  return autotune_impl(field, lo, hi, reps, 1);
 }
 
 int gsn_tuning_save(const char* path) {
@@ -173,16 +260,18 @@ int gsn_tuning_save(const char* path) {
   const bool have = cudaGetDeviceProperties(&prop, dev) == cudaSuccess;
   f << "{\n  \"device\": \"" << (have ? prop.name : "unknown") << "\",\n  \"plans\": [\n";
   bool first = true;
-  for (int field = 0; field < 3; ++field) {
-    const FieldOps* F = field_ops(field);
-    for (int k = 0; k <= F->max_log_n; ++k) {
-      Plan p;
-      if (!get_tuned_plan(field, k, &p)) continue;
-      auto it = g_tuned_ms.find({field, k});
-      f << (first ? "" : ",\n") << "    " << plan_json(field, p, it == g_tuned_ms.end() ? -1.0f : it->second);
-      first = false;
+  for (int mode = 0; mode < 2; ++mode)
+    for (int field = 0; field < 3; ++field) {
+      const FieldOps* F = field_ops(field);
+      for (int k = 0; k <= F->max_log_n; ++k) {
+        Plan p;
+        if (!get_tuned_plan(field, k, &p, mode)) continue;
+        auto it = g_tuned_ms.find(std::make_tuple(field, k, mode));
+        f << (first ? "" : ",\n") << "    "
+          << plan_json(field, p, it == g_tuned_ms.end() ? -1.0f : it->second, mode);
+        first = false;
+      }
     }
-  }
   f << "\n  ]\n}\n";
   return f.good() ? GSN_OK : set_error(GSN_ERR_ARG, "write failed for %s", path);
 }
@@ -211,9 +300,11 @@ int gsn_tuning_load(const char* path) {
       continue;
     find_int(obj, "kernel", &p.kernel);
     find_int(obj, "e_log", &p.e_log);
+    int mode = 0;
+    find_int(obj, "mode", &mode);
     const FieldOps* F = field_ops(field);
-    if (!F || !plan_valid(*F, p)) continue;
-    set_tuned_plan(field, p.log_n, p);
+    if (!F || !plan_valid(*F, p) || mode < 0 || mode > 1) continue;
+    set_tuned_plan(field, p.log_n, p, mode);
     ++loaded;
   }
   return loaded > 0 ? GSN_OK : set_error(GSN_ERR_ARG, "no valid plans in %s", path);
@@ -230,7 +321,7 @@ int gsn_plan_describe(int field, uint32_t log_n, char* buf, size_t len) {
   if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);
   if (!buf || !len) return set_error(GSN_ERR_ARG, "null buffer");
   const Plan p = plan_for(*F, (int)log_n);
-  const std::string s = plan_json(field, p, -1.0f);
+  const std::string s = plan_json(field, p, -1.0f, 0);
   std::snprintf(buf, len, "%s", s.c_str());
   return s.size() < len ? GSN_OK : set_error(GSN_ERR_ARG, "buffer too small");
 }

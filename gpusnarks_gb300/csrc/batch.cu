@@ -37,6 +37,7 @@ struct gsn_batch {
   uint64_t device_bytes = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  long long wait_cycles = 0;  // bounded-wait limit per dependency (0: default, ~1 s)
 };
 
 namespace gsn {
@@ -57,7 +58,7 @@ uint64_t job_scratch_bytes(const FieldOps& F, const Plan& p) {
   return p.npass > 1 ? ((uint64_t)1 << p.log_n) * F.limbs * sizeof(uint32_t) : 0;
 }
 
-int plan_batch(const FieldOps& F, const gsn_batch_job* jobs, size_t njobs, BatchPlan* out) {
+int plan_batch(const FieldOps& F, const gsn_batch_job* jobs, size_t njobs, BatchPlan* out, const Plan* force) {
   const uintptr_t align = (F.limbs % 4 == 0) ? 16 : 4;
   out->plans.resize(njobs);
   out->jobs.resize(njobs);
@@ -72,7 +73,8 @@ int plan_batch(const FieldOps& F, const gsn_batch_job* jobs, size_t njobs, Batch
     Tables T;
     int rc = resolve_tables(F, u.log_n, u.omega, u.dir, u.shift, &T, nullptr);
     if (rc) return rc;
-    Plan p = plan_for(F, (int)u.log_n, /*batched=*/true);
+    Plan p = force ? *force : plan_for(F, (int)u.log_n, /*batched=*/true);
+    if (force && p.log_n != (int)u.log_n) return set_error(GSN_ERR_ARG, "forced plan size mismatch");
     out->plans[i] = p;
     BatchJob& J = out->jobs[i];
     std::memset(&J, 0, sizeof(J));
@@ -115,7 +117,7 @@ static int enqueue_batch(gsn_batch* b, cudaStream_t s) {
   GSN_CUDA(cudaMemsetAsync(b->counters_dev, 0, b->counters_bytes, s));
   GSN_CUDA(cudaMemsetAsync(b->status_dev, 0, sizeof(uint32_t), s));
   cudaError_t e = b->F->batch(b->jobs_dev, b->work_dev, b->nwork, b->counters_dev, b->status_dev, b->grid,
-                              b->block, b->smem, s);
+                              b->block, b->smem, s, b->wait_cycles);
   if (e != cudaSuccess) return cuda_fail(e, "batch kernel launch");
   return GSN_OK;
 }
@@ -270,6 +272,61 @@ int gsn_batch_destroy(gsn_batch* b) {
   cudaDeviceSynchronize();
   batch_free(b);
   return GSN_OK;
+}
+
+int gsn_batch_selftest_wait(int field, int drop_first_pass, uint32_t* status_out) {
+  const FieldOps* F = field_ops(field);
+  if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);
+  if (!status_out) return set_error(GSN_ERR_ARG, "null output");
+  const uint32_t log_n = 12;
+  const size_t bytes = ((size_t)1 << log_n) * F->limbs * sizeof(uint32_t);
+  uint32_t *data = nullptr, *scratch = nullptr, *counters = nullptr, *status = nullptr;
+  BatchJob* jobs_dev = nullptr;
+  uint64_t* work_dev = nullptr;
+  gsn_batch_job u{};
+  BatchPlan bp;
+  int rc = dev_alloc((void**)&data, bytes);
+  if (!rc) rc = dev_alloc((void**)&scratch, bytes);
+  if (!rc) {
+    cudaMemset(data, 0, bytes);
+    u.data = data;
+    u.log_n = log_n;
+    u.dir = GSN_FORWARD;
+    rc = plan_batch(*F, &u, 1, &bp);
+  }
+  if (!rc && bp.plans[0].npass < 2) rc = set_error(GSN_ERR_STATE, "self-test needs a multi-pass plan");
+  if (!rc) {
+    bp.jobs[0].scratch = scratch;
+    std::vector<uint64_t> work;
+    for (uint64_t w : bp.work)
+      if (!drop_first_pass || ((w >> 28) & 0xF) != 0) work.push_back(w);
+    const size_t cbytes = (1 + kMaxPasses) * sizeof(uint32_t);
+    rc = dev_alloc((void**)&jobs_dev, sizeof(BatchJob));
+    if (!rc) rc = dev_alloc((void**)&work_dev, work.size() * sizeof(uint64_t));
+    if (!rc) rc = dev_alloc((void**)&counters, cbytes);
+    if (!rc) rc = dev_alloc((void**)&status, sizeof(uint32_t));
+    if (!rc) {
+      cudaMemcpy(jobs_dev, bp.jobs.data(), sizeof(BatchJob), cudaMemcpyHostToDevice);
+      cudaMemcpy(work_dev, work.data(), work.size() * sizeof(uint64_t), cudaMemcpyHostToDevice);
+      cudaMemset(counters, 0, cbytes);
+      cudaMemset(status, 0, sizeof(uint32_t));
+      // a short limit (~1 ms): with the first pass dropped nothing ever
+      // completes it, so every second-pass tile's wait must run out
+      cudaError_t e = F->batch(jobs_dev, work_dev, work.size(), counters, status, 8, bp.block, bp.smem, nullptr,
+                               2LL * 1000 * 1000);
+      if (e == cudaSuccess) e = cudaDeviceSynchronize();
+      if (e == cudaSuccess) e = cudaMemcpy(status_out, status, sizeof(uint32_t), cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) rc = cuda_fail(e, "batch wait self-test");
+      count_launches(1);
+    }
+  }
+  dev_free(data);
+  dev_free(scratch);
+  dev_free(jobs_dev);
+  dev_free(work_dev);
+  dev_free(counters);
+  dev_free(status);
+  return rc;
 }
 
 int gsn_fill_random(int field, uint32_t* data, uint64_t n, uint64_t seed, void* stream) {

@@ -23,7 +23,7 @@ struct FieldOps {
   cudaError_t (*fill)(uint32_t* out, uint64_t n, uint64_t seed, cudaStream_t s);
   cudaError_t (*batch)(const BatchJob* jobs_dev, const uint64_t* work_dev, uint64_t nwork,
                        uint32_t* counters_dev, uint32_t* status_dev, int grid, int block, size_t smem,
-                       cudaStream_t s);
+                       cudaStream_t s, long long wait_cycles /* <= 0: default (~1 s) */);
   int (*batch_occupancy)(int block, size_t smem);
   // host (canonical limbs in/out)
   void (*root)(int log_n, uint32_t* out);

@@ -282,10 +282,11 @@ __global__ void pointwise_mul_kernel(uint32_t* a, const uint32_t* b, uint64_t n)
 // counters[1 + job*kMaxPasses + p-1] reaches the tile count of pass p-1 of
 // that job.  Those tiles hold smaller tickets, so they are already claimed by
 // running CTAs that wait only on even smaller tickets: the waits always end.
-// Each wait is still bounded (kWaitBudgetCycles); on expiry the CTA records
-// GSN timeout in *status and carries on, so the launch always terminates.
+// Each wait is still bounded (wait_cycles of clock64, kWaitBudgetCycles by
+// default); on expiry the CTA records GSN_ERR_TIMEOUT in *status and carries
+// on, so the launch always terminates.
 // ---------------------------------------------------------------------------
-constexpr long long kWaitBudgetCycles = 8LL * 1000 * 1000 * 1000;  // ~4 s at 2 GHz
+constexpr long long kWaitBudgetCycles = 2LL * 1000 * 1000 * 1000;  // ~1 s at 2 GHz
 
 __device__ __forceinline__ uint32_t ld_volatile_u32(const uint32_t* p) {
   uint32_t v;
@@ -320,7 +321,7 @@ __device__ __forceinline__ void job_pass_args(PassArgs& A, const BatchJob& J, in
 
 template <class P>
 __global__ void batch_kernel(const BatchJob* __restrict__ jobs, const uint64_t* __restrict__ work,
-                             uint64_t nwork, uint32_t* counters, uint32_t* status) {
+                             uint64_t nwork, uint32_t* counters, uint32_t* status, long long wait_cycles) {
   extern __shared__ uint4 gsn_smem[];
   uint32_t* sm = reinterpret_cast<uint32_t*>(gsn_smem);
   __shared__ uint32_t s_ticket;
@@ -342,7 +343,7 @@ __global__ void batch_kernel(const BatchJob* __restrict__ jobs, const uint64_t* 
         const uint32_t* cnt = &counters[1 + (uint64_t)job * kMaxPasses + pass - 1];
         const long long start = clock64();
         while (ld_volatile_u32(cnt) < need) {
-          if (clock64() - start > kWaitBudgetCycles) {
+          if (clock64() - start > wait_cycles) {
             atomicExch(status, 8u);  // GSN_ERR_TIMEOUT
             break;
           }
@@ -385,13 +386,14 @@ struct Kernels {
   }
   static cudaError_t batch(const BatchJob* jobs_dev, const uint64_t* work_dev, uint64_t nwork,
                            uint32_t* counters_dev, uint32_t* status_dev, int grid, int block, size_t smem,
-                           cudaStream_t s) {
+                           cudaStream_t s, long long wait_cycles) {
     auto k = batch_kernel<P>;
     if (smem > kDefaultSmemOptIn) {
       cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
       if (e != cudaSuccess) return e;
     }
-    k<<<grid, block, smem, s>>>(jobs_dev, work_dev, nwork, counters_dev, status_dev);
+    k<<<grid, block, smem, s>>>(jobs_dev, work_dev, nwork, counters_dev, status_dev,
+                                wait_cycles > 0 ? wait_cycles : kWaitBudgetCycles);
     return cudaGetLastError();
   }
   static int batch_occupancy(int block, size_t smem) {

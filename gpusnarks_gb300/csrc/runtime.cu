@@ -143,19 +143,20 @@ Plan make_plan(const FieldOps& F, int log_n, int max_r, int target_j, int max_bl
 }
 
 static std::mutex g_plan_mu;
-static std::map<std::pair<int, int>, Plan> g_tuned;
+// (field, log_n, mode) -> plan; mode 0 = single transforms, 1 = batched kernel
+static std::map<std::tuple<int, int, int>, Plan> g_tuned;
 
-void set_tuned_plan(int field, int log_n, const Plan& p) {
+void set_tuned_plan(int field, int log_n, const Plan& p, int mode) {
   std::lock_guard<std::mutex> g(g_plan_mu);
-  g_tuned[{field, log_n}] = p;
+  g_tuned[std::make_tuple(field, log_n, mode)] = p;
 }
 void clear_tuned_plans() {
   std::lock_guard<std::mutex> g(g_plan_mu);
   g_tuned.clear();
 }
-bool get_tuned_plan(int field, int log_n, Plan* out) {
+bool get_tuned_plan(int field, int log_n, Plan* out, int mode) {
   std::lock_guard<std::mutex> g(g_plan_mu);
-  auto it = g_tuned.find({field, log_n});
+  auto it = g_tuned.find(std::make_tuple(field, log_n, mode));
   if (it == g_tuned.end()) return false;
   *out = it->second;
   return true;
@@ -187,7 +188,12 @@ Plan make_p32_plan(int log_n, int max_r, int log_j, int e_log) {
 
 Plan plan_for(const FieldOps& F, int log_n, bool batched) {
   Plan p;
-  if (get_tuned_plan(F.id, log_n, &p) && plan_valid(F, p) && !(batched && p.kernel != kKernelGeneric)) return p;
+  // batched plans come from their own table: a persistent launch runs every
+  // tile with the batch's largest block, so it wants wider tiles than a
+  // lone transform does
+  const int mode = batched ? 1 : 0;
+  if (get_tuned_plan(F.id, log_n, &p, mode) && plan_valid(F, p) && (!batched || p.kernel == kKernelGeneric))
+    return p;
   if (F.id == GSN_P32 && !batched && log_n >= 8) {
     // tiles of at most 2^14 elements (64 KB): J = 8 columns, radix <= 2^11
     p = make_p32_plan(log_n, 11, 3, 4);

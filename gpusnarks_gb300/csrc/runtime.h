@@ -51,9 +51,10 @@ Plan make_p32_plan(int log_n, int max_r, int log_j, int e_log);
 Plan make_plan(const FieldOps& F, int log_n, int max_r, int target_j, int max_block);
 bool plan_valid(const FieldOps& F, const Plan& p);
 size_t plan_smem_bytes(const FieldOps& F, const Plan& p, int pass);
-void set_tuned_plan(int field, int log_n, const Plan& p);
+// mode 0: plans for single transforms; mode 1: plans for the batched kernel
+void set_tuned_plan(int field, int log_n, const Plan& p, int mode = 0);
 void clear_tuned_plans();
-bool get_tuned_plan(int field, int log_n, Plan* out);
+bool get_tuned_plan(int field, int log_n, Plan* out, int mode = 0);
 
 // Resolved twiddle / coset tables for one transform.
 struct Tables {
@@ -94,7 +95,10 @@ struct BatchPlan {
   size_t smem = 0;
   uint64_t elements = 0;
 };
-int plan_batch(const FieldOps& F, const struct gsn_batch_job* jobs, size_t njobs, BatchPlan* out);
+// force: when non-null, every job uses this plan (the autotuner times
+// candidate plans this way); otherwise plan_for(..., batched=true).
+int plan_batch(const FieldOps& F, const struct gsn_batch_job* jobs, size_t njobs, BatchPlan* out,
+               const Plan* force = nullptr);
 uint64_t job_scratch_bytes(const FieldOps& F, const Plan& p);
 
 // Library-owned per-stream scratch (grow-only).

@@ -266,7 +266,7 @@ void launch(gsn_server* S, int si) {
   if (e == cudaSuccess) e = cudaMemsetAsync(sl.status_dev, 0, sizeof(uint32_t), sl.stream);
   if (e == cudaSuccess)
     e = F->batch(sl.jobs_dev, sl.work_dev, bp.work.size(), sl.counters_dev, sl.status_dev, grid, bp.block, bp.smem,
-                 sl.stream);
+                 sl.stream, 0);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(sl.status_host, sl.status_dev, sizeof(uint32_t), cudaMemcpyDeviceToHost, sl.stream);
   if (e == cudaSuccess) e = cudaEventRecord(sl.done, sl.stream);

@@ -132,6 +132,12 @@ int gsn_batch_status(gsn_batch* b);
 /* njobs, work items (tiles), total elements, device bytes held */
 int gsn_batch_info(gsn_batch* b, uint64_t* njobs, uint64_t* nwork, uint64_t* elements, uint64_t* device_bytes);
 int gsn_batch_destroy(gsn_batch* b);
+/* Self-test of the batch kernel's bounded dependency wait: one 2^12 job with
+ * a ~1 ms wait limit.  drop_first_pass = 1 leaves its first pass out of the
+ * work queue, so every later tile's wait must expire: *status_out becomes
+ * GSN_ERR_TIMEOUT and the launch still ends.  drop_first_pass = 0 is the
+ * control (*status_out = GSN_OK). */
+int gsn_batch_selftest_wait(int field, int drop_first_pass, uint32_t* status_out);
 
 /* ---- autotuning (no reference counterpart: the reference hard-codes 1024
  * chunks of 64 points, cuda/fft_kernel.cu:56-59) --------------------------- */
@@ -140,6 +146,10 @@ int gsn_batch_destroy(gsn_batch* b);
  * for every log_n in [lo, hi] on the current device, `reps` timed runs each,
  * and keeps the fastest for later transforms, batches and the server. */
 int gsn_autotune(int field, uint32_t log_n_lo, uint32_t log_n_hi, int reps);
+/* Same for the batched kernel: candidates are timed inside the persistent
+ * launch on a GPU-filling set of equal jobs; the winners are used by
+ * gsn_batch_create and the server. */
+int gsn_autotune_batch(int field, uint32_t log_n_lo, uint32_t log_n_hi, int reps);
 int gsn_tuning_save(const char* path); /* JSON */
 int gsn_tuning_load(const char* path);
 int gsn_tuning_clear(void);

@@ -80,6 +80,21 @@ def test_device_random_matches_host_replica(gsn, cuda_device):
         assert np.array_equal(gsn.to_host(d).reshape(f.shape(1000)), f.device_random(1000, 1234))
 
 
+@pytest.mark.parametrize("fid", [0, 1, 2])
+def test_bounded_wait_expires_without_fault(gsn, cuda_device, fid):
+    """Failure detection on the GPU without a fault: a batch whose first pass
+    is missing from the queue can never satisfy its dependency; every wait
+    runs out after ~1 ms, the kernel records GSN_ERR_TIMEOUT and ends, and the
+    context stays usable (the control run right after succeeds)."""
+    import ctypes
+    lib = gsn.load()
+    st = ctypes.c_uint32(123)
+    assert lib.gsn_batch_selftest_wait(fid, 1, ctypes.byref(st)) == 0, lib.gsn_last_error()
+    assert st.value == 8  # GSN_ERR_TIMEOUT
+    assert lib.gsn_batch_selftest_wait(fid, 0, ctypes.byref(st)) == 0, lib.gsn_last_error()
+    assert st.value == 0
+
+
 def test_batch_rejects_bad_jobs(gsn, cuda_device):
     import torch
     from gpusnarks_gb300.batch import Batch
