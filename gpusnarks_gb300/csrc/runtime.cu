@@ -357,6 +357,22 @@ int resolve_tables(const FieldOps& F, uint32_t log_n, const uint32_t* omega, int
   return GSN_OK;
 }
 
+bool find_default_twiddles(const FieldOps& F, int log_n, const uint32_t** tw, int* tw_log) {
+  TableCache& C = cache();
+  std::lock_guard<std::mutex> g(C.mu);
+  for (int k = log_n; k <= F.max_log_n; ++k) {
+    uint32_t r[kMaxLimbs];
+    default_root(F, k, r);
+    auto it = C.powers.find(std::make_tuple(F.id, k, limbs_key(r, F.limbs)));
+    if (it != C.powers.end()) {
+      *tw = static_cast<const uint32_t*>(it->second.p);
+      *tw_log = k;
+      return true;
+    }
+  }
+  return false;
+}
+
 int resolve_p32_tables(const FieldOps& F, const Plan& plan, Tables* T) {
   uint32_t root[kMaxLimbs];
   std::memcpy(root, T->root, sizeof(uint32_t) * F.limbs);

@@ -73,6 +73,10 @@ struct Tables {
   int p32_lo_bits = 0;
 };
 
+// Looks up an already built default-root twiddle table covering 2^log_n
+// without building one (no allocation); false when none is cached.
+bool find_default_twiddles(const FieldOps& F, int log_n, const uint32_t** tw, int* tw_log);
+
 // Compact per-radix and two-level four-step tables for a kKernelP32 plan.
 int resolve_p32_tables(const FieldOps& F, const Plan& plan, Tables* T);
 

@@ -88,6 +88,18 @@ int gsn_ntt(int field, uint32_t* data, uint32_t log_n, const uint32_t* omega, in
 int gsn_ntt_scratch(int field, uint32_t* data, uint32_t log_n, const uint32_t* omega, int dir,
                     const uint32_t* shift, uint32_t* scratch, void* stream);
 
+/* Same transform without allocating device memory (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc when they run a
+ * transform (inside a stream capture, in a loop that must not synchronise,
+ * or with device memory owned by another allocator).  The scratch is one
+ * fixed 64 MiB array inside the library, so n * limbs * 4 must not exceed
+ * 64 MiB (2^24 p32, 2^21 BLS12-381, 2^19 MNT4-753 elements); only GSN_FORWARD
+ * and GSN_INVERSE with the default root.  gsn_prepare(field, log_n, NULL)
+ * must have run first (GSN_ERR_STATE otherwise).  The first call on a device
+ * looks up the array's address, so make it before any stream capture.  All
+ * calls share the array: calls that overlap on the GPU race. */
+int gsn_ntt_noalloc(int field, uint32_t* data, uint32_t log_n, int dir, void* stream);
+
 /* best_fft drop-in: `data` is host memory (pageable or pinned), transformed
  * in place; host->device copy, transform, device->host copy; returns when the
  * result is back in `data`.  Unlike cuda/fft_kernel.cu:144-174 it honours
