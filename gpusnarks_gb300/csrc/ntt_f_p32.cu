@@ -8,6 +8,8 @@ namespace gsn {
 const FieldOps kOpsP32 = make_field_ops<FieldP32>(28, 16);
 
 cudaError_t launch_p32_pass(const P32Args& A, int e_log, int block, int grid_cap, cudaStream_t s) {
-  return P32Kernels::launch(A, e_log, block, grid_cap, s);
+  if (e_log == 3) return p32_launch_et<3>(A, block, grid_cap, s);
+  if (e_log == 4) return p32_launch_et<4>(A, block, grid_cap, s);
+  return cudaErrorInvalidValue;
 }
 }  // namespace gsn

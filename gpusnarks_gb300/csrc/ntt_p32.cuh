@@ -240,32 +240,202 @@ __global__ void __launch_bounds__(512) ntt_p32_kernel(P32Args A) {
   }
 }
 
-struct P32Kernels {
-  template <int ET, int LCG>
-  static cudaError_t launch_one(const P32Args& A, int block, int grid_cap, cudaStream_t s) {
-    const size_t smem = ((size_t)1 << (A.log_r + A.log_j)) * sizeof(uint32_t);
-    auto k = ntt_p32_kernel<ET, LCG>;
-    if (smem > kDefaultSmemOptIn) {
-      cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-    }
-    const uint64_t grid = A.tiles < (uint64_t)grid_cap ? A.tiles : (uint64_t)grid_cap;
-    k<<<(unsigned)grid, block, smem, s>>>(A);
-    return cudaGetLastError();
+// ---------------------------------------------------------------------------
+// Fixed-radix variant: the pass radix 2^RL is a template parameter, so the
+// whole sub-step schedule unrolls at compile time.  The swizzle map is linear
+// over GF(2) (shifts and XORs) and the rows of one register group differ from
+// their base row only in bits the base row does not use, so a row's chunk is
+// the thread's base chunk XOR a compile-time constant; twiddle offsets become
+// load immediates.  Same arithmetic, layout and results as ntt_p32_kernel.
+// ---------------------------------------------------------------------------
+namespace p32 {
+
+// chunk_of(row, 0) as a constant expression (chunk_of(row, cg) = chunk_c(row) ^ cg)
+template <int LCG>
+__host__ __device__ constexpr uint32_t chunk_c(uint32_t row) {
+  constexpr int SH = 3 - LCG;
+  uint32_t x = row >> SH;
+  if (SH == 1) {
+    x ^= x >> 8;
+    x ^= x >> 4;
+    x ^= x >> 2;
+    x ^= x >> 1;
+  } else if (SH == 2) {
+    x ^= x >> 8;
+    x ^= x >> 4;
+    x ^= x >> 2;
+  } else {
+    x ^= x >> 9;
+    x ^= x >> 6;
+    x ^= x >> 3;
   }
-  static cudaError_t launch(const P32Args& A, int e_log, int block, int grid_cap, cudaStream_t s) {
-    const int lcg = A.log_j - 2;
-    if (e_log == 3) {
-      if (lcg == 0) return launch_one<3, 0>(A, block, grid_cap, s);
-      if (lcg == 1) return launch_one<3, 1>(A, block, grid_cap, s);
-      if (lcg == 2) return launch_one<3, 2>(A, block, grid_cap, s);
-    } else if (e_log == 4) {
-      if (lcg == 0) return launch_one<4, 0>(A, block, grid_cap, s);
-      if (lcg == 1) return launch_one<4, 1>(A, block, grid_cap, s);
-      if (lcg == 2) return launch_one<4, 2>(A, block, grid_cap, s);
+  return (row << LCG) ^ ((x & ((1u << SH) - 1u)) << LCG);
+}
+
+template <int ET, int LS, int S0, int LCG>
+__device__ __forceinline__ void substep_fixed(uint4* sm, const uint32_t* __restrict__ twt, uint32_t base_chunk,
+                                              uint32_t low) {
+  constexpr int E = 1 << ET;
+  uint4 x[E];
+#pragma unroll
+  for (int m = 0; m < E; ++m) x[m] = sm[base_chunk ^ chunk_c<LCG>((uint32_t)m << LS)];
+#pragma unroll
+  for (int q = 0; q < ET; ++q) {
+    const uint32_t* tq = twt + (low << (S0 + q));
+#pragma unroll
+    for (int t = 0; t < (E >> (q + 1)); ++t) {
+      const uint32_t w = __ldg(tq + ((uint32_t)t << (LS + S0 + q)));
+#pragma unroll
+      for (int g = 0; g < (1 << q); ++g) {
+        const int m = g * (E >> q) + t;
+        bfly4(x[m], x[m + (E >> (q + 1))], w);
+      }
     }
-    return cudaErrorInvalidValue;
   }
-};
+#pragma unroll
+  for (int m = 0; m < E; ++m) sm[base_chunk ^ chunk_c<LCG>((uint32_t)m << LS)] = x[m];
+}
+
+template <int RL, int ET, int LCG, int S0>
+__device__ __forceinline__ void substeps_fixed(uint4* sm, const uint32_t* __restrict__ twt) {
+  if constexpr (S0 < RL) {
+    constexpr int et = (RL - S0 < ET) ? (RL - S0) : ET;
+    constexpr int ls = RL - S0 - et;
+    constexpr uint32_t units = (1u << (RL - et)) << LCG;
+    for (uint32_t u = threadIdx.x; u < units; u += blockDim.x) {
+      const uint32_t cg = u & ((1u << LCG) - 1u);
+      const uint32_t uu = u >> LCG;
+      const uint32_t low = uu & ((1u << ls) - 1u);
+      const uint32_t rowbase = ((uu >> ls) << (RL - S0)) | low;
+      substep_fixed<et, ls, S0, LCG>(sm, twt, chunk_c<LCG>(rowbase) ^ cg, low);
+    }
+    __syncthreads();
+    substeps_fixed<RL, ET, LCG, S0 + et>(sm, twt);
+  }
+}
+
+}  // namespace p32
+
+template <int RL, int ET, int LCG>
+__global__ void __launch_bounds__(512) ntt_p32_fixed_kernel(P32Args A) {
+  using namespace p32;
+  extern __shared__ uint4 gsn_smem[];
+  uint4* sm = gsn_smem;
+  constexpr uint32_t CG = 1u << LCG;
+  constexpr uint32_t R = 1u << RL;
+  constexpr int lj = LCG + 2;
+
+  for (uint64_t tile = blockIdx.x; tile < A.tiles; tile += gridDim.x) {
+    uint64_t base = 0, jbase = 0, rowpre = 0, obase = 0;
+    int lo0 = 0;
+    if (!A.last) {
+      const int per_prefix_log = A.log_inner - lj;
+      const uint64_t prefix = tile >> per_prefix_log;
+      jbase = (tile & (((uint64_t)1 << per_prefix_log) - 1)) << lj;
+      base = (prefix << (RL + A.log_inner)) + jbase;
+    } else {
+      lo0 = (A.npass == 1) ? 0 : A.radix_log[0];
+      const int k0b_log = lo0 - lj;
+      const uint64_t rest = tile >> k0b_log;
+      const uint64_t k0 = (tile & (((uint64_t)1 << k0b_log) - 1)) << lj;
+      rowpre = (k0 << (A.log_outer - lo0)) + rest;
+      obase = k0 + (rest_offset(rest, A.npass, A.radix_log) << lo0);
+    }
+
+    if (!A.last) {
+      for (uint32_t v = threadIdx.x; v < R * CG; v += blockDim.x) {
+        const uint32_t k = v >> LCG, cg = v & (CG - 1);
+        const uint64_t g = base + ((uint64_t)k << A.log_inner) + 4 * cg;
+        uint4 x = __ldcg(reinterpret_cast<const uint4*>(A.src + g));
+        if (A.first) x = premul(A, x, g);
+        sm_st<LCG>(sm, k, cg, x);
+      }
+    } else {
+      const int row_stride_log = A.log_outer - lo0;
+      for (uint32_t v = threadIdx.x; v < (R >> 2) * CG; v += blockDim.x) {
+        const uint32_t jg = v & (CG - 1), k4 = v >> LCG;
+        uint4 rr[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const uint64_t jj = 4 * jg + i;
+          const uint64_t g = ((rowpre + (jj << row_stride_log)) << RL) + 4 * k4;
+          rr[i] = __ldcg(reinterpret_cast<const uint4*>(A.src + g));
+          if (A.first) rr[i] = premul(A, rr[i], g);
+        }
+        sm_st<LCG>(sm, 4 * k4 + 0, jg, make_uint4(rr[0].x, rr[1].x, rr[2].x, rr[3].x));
+        sm_st<LCG>(sm, 4 * k4 + 1, jg, make_uint4(rr[0].y, rr[1].y, rr[2].y, rr[3].y));
+        sm_st<LCG>(sm, 4 * k4 + 2, jg, make_uint4(rr[0].z, rr[1].z, rr[2].z, rr[3].z));
+        sm_st<LCG>(sm, 4 * k4 + 3, jg, make_uint4(rr[0].w, rr[1].w, rr[2].w, rr[3].w));
+      }
+    }
+    __syncthreads();
+
+    substeps_fixed<RL, ET, LCG, 0>(sm, A.tw_tile);  // ends with __syncthreads()
+
+    for (uint32_t v = threadIdx.x; v < R * CG; v += blockDim.x) {
+      const uint32_t k = v >> LCG, cg = v & (CG - 1);
+      uint4 x = sm_ld<LCG>(sm, brev(k, RL), cg);
+      if (!A.last) {
+        const uint64_t jp = jbase + 4 * cg;
+        const uint64_t ek = (uint64_t)k << A.log_outer;
+        uint4 w;
+        w.x = tw_n(A, jp * ek);
+        w.y = tw_n(A, (jp + 1) * ek);
+        w.z = tw_n(A, (jp + 2) * ek);
+        w.w = tw_n(A, (jp + 3) * ek);
+        x = mul4v(x, w);
+        *reinterpret_cast<uint4*>(A.dst + base + ((uint64_t)k << A.log_inner) + 4 * cg) = x;
+      } else {
+        const uint64_t opos = obase + 4 * cg + ((uint64_t)k << A.log_outer);
+        if (A.post_table) x = mul4v(x, __ldg(reinterpret_cast<const uint4*>(A.post_table + opos)));
+        *reinterpret_cast<uint4*>(A.dst + opos) = x;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// Launchers.  The kernels for one sub-step size ET are instantiated in one
+// translation unit each (ntt_p32_e3.cu, ntt_p32_e4.cu) so they compile in
+// parallel: fixed-radix kernels for radix 2^8..2^13 with 4 or 8 columns per
+// tile, the runtime-radix kernel for everything else.
+template <int ET>
+cudaError_t p32_launch_et(const P32Args& A, int block, int grid_cap, cudaStream_t s);
+
+#ifdef GSN_P32_INSTANTIATE_ET
+namespace p32 {
+template <class K>
+cudaError_t launch_kernel(K k, const P32Args& A, int block, int grid_cap, cudaStream_t s) {
+  const size_t smem = ((size_t)1 << (A.log_r + A.log_j)) * sizeof(uint32_t);
+  if (smem > kDefaultSmemOptIn) {
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return e;
+  }
+  const uint64_t grid = A.tiles < (uint64_t)grid_cap ? A.tiles : (uint64_t)grid_cap;
+  k<<<(unsigned)grid, block, smem, s>>>(A);
+  return cudaGetLastError();
+}
+template <int ET, int LCG, int RL>
+cudaError_t launch_fixed(const P32Args& A, int block, int grid_cap, cudaStream_t s) {
+  if constexpr (RL <= 13) {
+    if (A.log_r == RL) return launch_kernel(ntt_p32_fixed_kernel<RL, ET, LCG>, A, block, grid_cap, s);
+    return launch_fixed<ET, LCG, RL + 1>(A, block, grid_cap, s);
+  } else {
+    return launch_kernel(ntt_p32_kernel<ET, LCG>, A, block, grid_cap, s);
+  }
+}
+}  // namespace p32
+
+template <>
+cudaError_t p32_launch_et<GSN_P32_INSTANTIATE_ET>(const P32Args& A, int block, int grid_cap, cudaStream_t s) {
+  constexpr int ET = GSN_P32_INSTANTIATE_ET;
+  switch (A.log_j - 2) {
+    case 0: return p32::launch_fixed<ET, 0, 8>(A, block, grid_cap, s);
+    case 1: return p32::launch_fixed<ET, 1, 8>(A, block, grid_cap, s);
+    case 2: return p32::launch_kernel(ntt_p32_kernel<ET, 2>, A, block, grid_cap, s);
+    default: return cudaErrorInvalidValue;
+  }
+}
+#endif
 
 }  // namespace gsn
