@@ -121,6 +121,17 @@ def pointwise_mul(field, a, b, *, stream=None):
     return a
 
 
+TO_MONTGOMERY, FROM_MONTGOMERY, REVERSE_LIMBS = 0, 1, 2
+
+
+def convert(field, data, mode: int, *, stream=None):
+    """In place: enter / leave Montgomery form, or reverse each element's limb order."""
+    f = field_of(field)
+    n = data.numel() // f.limbs
+    check(load().gsn_convert(f.fid, data.data_ptr(), n, int(mode), _stream_handle(stream)))
+    return data
+
+
 def autotune(field, lo: int, hi: int, reps: int = 5, *, batched: bool = False) -> None:
     """Time candidate plans for every log n in [lo, hi] and keep the fastest
     (for single transforms, or for the persistent batched kernel)."""

@@ -45,6 +45,7 @@ _SIGNATURES = [
     ("gsn_prepare", ctypes.c_int, [ctypes.c_int, ctypes.c_uint32, _u32p]),
     ("gsn_pointwise_mul", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
                                          ctypes.c_void_p]),
+    ("gsn_convert", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p]),
     ("gsn_synchronize", ctypes.c_int, [ctypes.c_void_p]),
     ("gsn_host_alloc", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]),
     ("gsn_host_free", ctypes.c_int, [ctypes.c_void_p]),

@@ -292,7 +292,9 @@ int gsn_batch_selftest_wait(int field, int drop_first_pass, uint32_t* status_out
     u.data = data;
     u.log_n = log_n;
     u.dir = GSN_FORWARD;
-    rc = plan_batch(*F, &u, 1, &bp);
+    // two passes of radix 2^6, whatever the tuning table holds for 2^12
+    const Plan forced = make_plan(*F, (int)log_n, 6, 0, 128);
+    rc = plan_batch(*F, &u, 1, &bp, &forced);
   }
   if (!rc && bp.plans[0].npass < 2) rc = set_error(GSN_ERR_STATE, "self-test needs a multi-pass plan");
   if (!rc) {

@@ -48,6 +48,7 @@ constexpr FieldOps make_field_ops(int max_log_n, int default_tw_log) {
                   &Kernels<P>::powers,
                   &Kernels<P>::pointwise,
                   &Kernels<P>::fill,
+                  &Kernels<P>::convert,
                   &Kernels<P>::batch,
                   &Kernels<P>::batch_occupancy,
                   &HostOps<P>::root,

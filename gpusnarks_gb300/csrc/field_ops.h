@@ -21,6 +21,7 @@ struct FieldOps {
   cudaError_t (*powers)(uint32_t* out, uint64_t count, const uint32_t* base_canon, cudaStream_t s);
   cudaError_t (*pointwise)(uint32_t* a, const uint32_t* b, uint64_t n, cudaStream_t s);
   cudaError_t (*fill)(uint32_t* out, uint64_t n, uint64_t seed, cudaStream_t s);
+  cudaError_t (*convert)(uint32_t* data, uint64_t n, int mode, cudaStream_t s);
   cudaError_t (*batch)(const BatchJob* jobs_dev, const uint64_t* work_dev, uint64_t nwork,
                        uint32_t* counters_dev, uint32_t* status_dev, int grid, int block, size_t smem,
                        cudaStream_t s, long long wait_cycles /* <= 0: default (~1 s) */);

@@ -258,6 +258,33 @@ __global__ void fill_random_kernel(uint32_t* out, uint64_t n, uint64_t seed) {
   }
 }
 
+// Element format conversions, in place:
+//   mode 0: x -> x*R mod p      (enter Montgomery form: one product by R^2)
+//   mode 1: x -> x*R^-1 mod p   (leave Montgomery form: one product by 1)
+//   mode 2: reverse the limb order of each element (big-endian limb arrays,
+//           as the reference's cpu_fields::Field stores them, fields/field.h:48,56,
+//           <-> the little-endian im_rep of cuda/device_field.h:75)
+template <class P>
+__global__ void convert_kernel(uint32_t* data, uint64_t n, int mode) {
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    Fe<P> x, r;
+    fe_load<P>(x, data + i * P::N);
+    if (mode == 0) {
+      fe_to_mont<P>(r, x);
+    } else if (mode == 1) {
+      Fe<P> one;
+#pragma unroll
+      for (int j = 0; j < P::N; ++j) one.l[j] = j == 0 ? 1u : 0u;
+      fe_mul<P>(r, x, one);
+    } else {
+#pragma unroll
+      for (int j = 0; j < P::N; ++j) r.l[j] = x.l[P::N - 1 - j];
+    }
+    fe_store<P>(data + i * P::N, r);
+  }
+}
+
 // a[i] = a[i] * b[i] mod p (canonical in, canonical out): two Montgomery
 // products, the second by R^2.
 template <class P>
@@ -402,6 +429,14 @@ struct Kernels {
     int nb = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k, block, smem) != cudaSuccess) return 0;
     return nb;
+  }
+  static cudaError_t convert(uint32_t* data, uint64_t n, int mode, cudaStream_t s) {
+    const int block = 256;
+    uint64_t grid = (n + block - 1) / block;
+    if (grid > 152 * 64) grid = 152 * 64;
+    if (grid == 0) return cudaSuccess;
+    convert_kernel<P><<<(unsigned)grid, block, 0, s>>>(data, n, mode);
+    return cudaGetLastError();
   }
   static cudaError_t fill(uint32_t* out, uint64_t n, uint64_t seed, cudaStream_t s) {
     const int block = 256;

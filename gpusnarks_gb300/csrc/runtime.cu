@@ -623,6 +623,19 @@ int gsn_pointwise_mul(int field, uint32_t* a, const uint32_t* b, uint64_t n, voi
   return GSN_OK;
 }
 
+int gsn_convert(int field, uint32_t* data, uint64_t n, int mode, void* stream) {
+  const FieldOps* F = field_ops(field);
+  if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);
+  if (mode < GSN_TO_MONTGOMERY || mode > GSN_REVERSE_LIMBS) return set_error(GSN_ERR_ARG, "bad mode %d", mode);
+  int rc = check_data_ptr(*F, data);
+  if (rc) return rc;
+  if (n == 0) return GSN_OK;
+  cudaError_t e = F->convert(data, n, mode, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "convert launch");
+  count_launches(1);
+  return GSN_OK;
+}
+
 int gsn_synchronize(void* stream) {
   GSN_CUDA(cudaStreamSynchronize(static_cast<cudaStream_t>(stream)));
   return GSN_OK;

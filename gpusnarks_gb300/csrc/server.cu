@@ -20,6 +20,7 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cmath>
 #include <condition_variable>
 #include <cstring>
 #include <deque>
@@ -154,6 +155,13 @@ namespace {
 
 uint64_t elem_bytes(const FieldOps* F, uint32_t log_n) { return ((uint64_t)1 << log_n) * F->limbs * sizeof(uint32_t); }
 
+// Integer multiply-adds of one transform: (n/2) log2 n products of
+// 2 (2 s^2 + s) word multiply-adds each (s limbs).
+double request_work(const FieldOps* F, uint32_t log_n) {
+  const double s = F->limbs;
+  return std::ldexp(1.0, (int)log_n - 1) * std::max(1u, log_n) * 2.0 * (2.0 * s * s + s);
+}
+
 uint32_t* dptr(gsn_server* S, uint64_t off) { return reinterpret_cast<uint32_t*>(S->arena.base + off); }
 
 void free_mem(gsn_server* S, Req& q, bool data_too) {
@@ -222,11 +230,21 @@ void launch(gsn_server* S, int si) {
   // oldest ready request decides the field
   const FieldOps* F = S->reqs[S->ready.front()].F;
   const size_t cap = S->cfg.max_batch_jobs > 0 ? (size_t)S->cfg.max_batch_jobs : 4096;
+  const double work_cap = S->cfg.max_launch_work ? (double)S->cfg.max_launch_work : 4e10;
   std::vector<uint64_t> ids;
   std::deque<uint64_t> keep;
+  double work = 0;
   for (uint64_t id : S->ready) {
-    if (S->reqs[id].F == F && ids.size() < std::min(cap, kSlotJobs)) ids.push_back(id);
-    else keep.push_back(id);
+    const Req& q = S->reqs[id];
+    const double w = request_work(q.F, q.r.log_n);
+    // oldest first; stop packing once the launch holds work_cap (the first
+    // request always goes), so launches stay short and new arrivals start soon
+    if (q.F == F && ids.size() < std::min(cap, kSlotJobs) && (ids.empty() || work + w <= work_cap)) {
+      ids.push_back(id);
+      work += w;
+    } else {
+      keep.push_back(id);
+    }
   }
   std::vector<gsn_batch_job> jobs(ids.size());
   for (size_t i = 0; i < ids.size(); ++i) {

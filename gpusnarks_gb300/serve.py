@@ -14,7 +14,7 @@ from ._lib import check, load
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_int32),
-                ("max_batch_jobs", ctypes.c_int32)]
+                ("max_batch_jobs", ctypes.c_int32), ("max_launch_work", ctypes.c_uint64)]
 
 
 class Request(ctypes.Structure):
@@ -56,9 +56,10 @@ def _lib():
 
 
 class Server:
-    def __init__(self, hbm_budget_bytes: int, max_inflight: int = 4, max_batch_jobs: int = 0):
+    def __init__(self, hbm_budget_bytes: int, max_inflight: int = 4, max_batch_jobs: int = 0,
+                 max_launch_work: int = 0):
         self.lib = _lib()
-        cfg = ServerConfig(hbm_budget_bytes, max_inflight, max_batch_jobs)
+        cfg = ServerConfig(hbm_budget_bytes, max_inflight, max_batch_jobs, max_launch_work)
         h = ctypes.c_void_p()
         check(self.lib.gsn_server_create(ctypes.byref(cfg), ctypes.byref(h)))
         self.h = h

@@ -114,6 +114,16 @@ int gsn_prepare(int field, uint32_t log_n, const uint32_t* omega);
 /* a[i] = a[i] * b[i] mod p on device memory (canonical values). */
 int gsn_pointwise_mul(int field, uint32_t* a, const uint32_t* b, uint64_t n, void* stream);
 
+/* In-place element format conversion on device memory.
+ *   GSN_TO_MONTGOMERY    x -> x*R mod p      (R = 2^(32*LIMBS))
+ *   GSN_FROM_MONTGOMERY  x -> x*R^-1 mod p
+ *   GSN_REVERSE_LIMBS    reverse each element's limb order: big-endian limb
+ *                        arrays (the reference's cpu_fields::Field,
+ *                        fields/field.h:48,56) <-> the little-endian im_rep of
+ *                        cuda/device_field.h:75. */
+enum { GSN_TO_MONTGOMERY = 0, GSN_FROM_MONTGOMERY = 1, GSN_REVERSE_LIMBS = 2 };
+int gsn_convert(int field, uint32_t* data, uint64_t n, int mode, void* stream);
+
 /* ---- batched transforms (no reference counterpart: the reference runs one
  * transform per best_fft call) --------------------------------------------- */
 
@@ -181,6 +191,10 @@ typedef struct gsn_server_config {
   uint64_t hbm_budget_bytes; /* device bytes for polynomials + scratch            */
   int32_t max_inflight;      /* persistent launches in flight at once (>= 1)      */
   int32_t max_batch_jobs;    /* cap on requests per launch (0 = 4096)             */
+  uint64_t max_launch_work;  /* cap on the integer multiply-adds packed into one
+                                launch, (n/2) log2 n x 2(2s^2+s) per request;
+                                the oldest ready request always goes
+                                (0 = 4e10, a few milliseconds of GPU time)       */
 } gsn_server_config;
 
 typedef struct gsn_request {
