@@ -190,6 +190,18 @@ def time_e2e_host(g, f, log_n: int, steps: int, warmup: int):
     return times, nbytes
 
 
+def profiled_traffic(key: str):
+    """DRAM bytes per launch (dram__bytes_read.sum + dram__bytes_write.sum) recorded from an ncu capture
+    in profiles/traffic.txt (`<kernel> <size>: <bytes>` lines); None when absent."""
+    path = ROOT / "profiles" / "traffic.txt"
+    if not path.exists():
+        return None
+    for ln in path.read_text().splitlines():
+        if ln.startswith(key + ":"):
+            return int(ln.split(":", 1)[1].split()[0])
+    return None
+
+
 def imad_work(f, log_n: int) -> float:
     s = f.limbs
     per_mul = 2 * (2 * s * s + s)
@@ -208,6 +220,7 @@ def p32_sweep(g, torch, flush, hbm_gbs, steps=5):
         out[f"2^{log_n}"] = {"ms": round(t * 1e3, 4), "Melem_s": round(n / t / 1e6, 1),
                              "hbm_frac": round(B / t / 1e9 / hbm_gbs, 4),
                              "single_pass_frac": round(8 * n / t / 1e9 / hbm_gbs, 4), "p_min": pmin}
+    out["2^26"]["dram_bytes_per_launch"] = profiled_traffic("ntt_p32_fixed_kernel 2^26")
     return out
 
 
@@ -279,7 +292,10 @@ def run_gpu(args, rank, local, ws):
     t_total = max_over_ranks(sum(ts), ws)
     t_step = t_total / args.steps
     value = n * args.steps * ws / t_total / 1e6
-    achieved = imad_work(f, log_n) / t_step
+    # One step is `per_step` launches of the pass kernel; per launch, the algorithmic work is the
+    # step's work / per_step and the average duration the step time / per_step.
+    per_step = max(1, int(launches) // args.steps)
+    achieved = (imad_work(f, log_n) / per_step) / (t_step / per_step)
 
     # e2e through the host entry point
     e2e_ts, nbytes = time_e2e_host(g, f, log_n, args.steps, max(1, args.warmup // 2))
@@ -300,19 +316,15 @@ def run_gpu(args, rank, local, ws):
                      "frac": round(achieved / ip["mads_per_s"], 4), "traffic": None,
                      "peak_source": "gsn_microbench_imad in this process (PTX mad.lo.cc/madc.hi.cc chains, "
                                     "all SMs, full occupancy)",
-                     "algorithmic_work": "2352 IMAD per 24-limb Montgomery product x (n/2) log2 n"},
+                     "algorithmic_work": "2352 IMAD per 24-limb Montgomery product x (n/2) log2 n",
+                     "launches_per_step": per_step},
         "gpu_launches": int(launches),
         "clocks": clk.summary(),
         "published_reference": {"what": "FFT 768-bit n=2^18, GTX 1060, reference dataflow (not a DFT)",
                                 "seconds": PUBLISHED_REF_768_2_18_S,
                                 "Melem_s": round(n / PUBLISHED_REF_768_2_18_S / 1e6, 5)},
     }
-    trf = ROOT / "profiles" / "traffic.json"
-    if trf.exists():
-        try:
-            line["roofline"]["traffic"] = json.loads(trf.read_text()).get("mnt4753_fr_2^18_bytes_per_step")
-        except Exception:
-            pass
+    line["roofline"]["traffic"] = profiled_traffic("ntt_pass_kernel<FieldMNT4_753> 2^18")
     if rank == 0 and ws == 1:
         line["cpu_baseline"] = cpu_baseline(args)
     if not args.headline_only and rank == 0:

@@ -55,6 +55,8 @@ _SIGNATURES = [
                                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
     ("gsn_microbench_mont", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_double)]),
+    ("gsn_microbench_mont_coop", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                ctypes.POINTER(ctypes.c_double)]),
     ("gsn_batch_create", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_void_p)]),
     ("gsn_batch_launch", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),

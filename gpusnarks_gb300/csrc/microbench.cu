@@ -14,7 +14,10 @@
 #include <cstdint>
 #include <vector>
 
+#include <cstring>
+
 #include "arith.cuh"
+#include "host_field.h"
 #include "gpusnarks_gb300.h"
 #include "runtime.h"
 
@@ -128,9 +131,221 @@ static int run_mont_bench(int iters, double* muls_per_s) {
   return GSN_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Cooperative Montgomery product: one element spread over TPI lanes of a warp,
+// lane t holding limbs [tL, tL + L), L = N / TPI.  CIOS row i: every lane adds
+// its slice of a * b_i and of p * m into a window of L + 2 words anchored at
+// limb tL (windows of neighbouring lanes overlap by two words); m comes from
+// lane 0 by shuffle; the shift by one limb hands each lane's lowest word to
+// the lane below.  After N rows the overlaps are folded upwards in TPI - 1
+// rounds.  Output in [0, 2p) (lazy: 4p < R for the fields it is used with).
+// ---------------------------------------------------------------------------
+template <class P, int TPI>
+struct Coop {
+  static constexpr int N = P::N;
+  static constexpr int L = N / TPI;
+  static_assert(N % TPI == 0, "limbs must split evenly");
+
+  __device__ static void load_mod(uint32_t (&pl)[L], int lane) {
+#pragma unroll
+    for (int j = 0; j < L; ++j) {
+      uint32_t v = 0;
+#pragma unroll
+      for (int t = 0; t < TPI; ++t)
+        if (t == lane) v = P::mod(t * L + j);
+      pl[j] = v;
+    }
+  }
+
+  // acc[0..L+1] += x[0..L) * y
+  __device__ static void row(uint32_t (&acc)[L + 2], const uint32_t (&x)[L], uint32_t y) {
+    ptx::mad_lo_cc(acc[0], x[0], y, acc[0]);
+#pragma unroll
+    for (int j = 1; j < L; ++j) ptx::madc_lo_cc(acc[j], x[j], y, acc[j]);
+    ptx::addc_cc(acc[L], acc[L], 0u);
+    ptx::addc(acc[L + 1], acc[L + 1], 0u);
+    ptx::mad_hi_cc(acc[1], x[0], y, acc[1]);
+#pragma unroll
+    for (int j = 1; j < L; ++j) ptx::madc_hi_cc(acc[j + 1], x[j], y, acc[j + 1]);
+    ptx::addc(acc[L + 1], acc[L + 1], 0u);
+  }
+
+  // r = a * b * R^-1 (mod p, in [0, 2p)); a, r distributed; b: all N limbs.
+  __device__ static void mul(uint32_t (&r)[L], const uint32_t (&a)[L], const uint32_t (&b)[N],
+                             const uint32_t (&pl)[L], int lane, unsigned mask) {
+    uint32_t acc[L + 2];
+#pragma unroll
+    for (int j = 0; j < L + 2; ++j) acc[j] = 0u;
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      row(acc, a, b[i]);
+      const uint32_t m = __shfl_sync(mask, acc[0] * P::PINV, 0, TPI);
+      row(acc, pl, m);
+      uint32_t nxt = __shfl_down_sync(mask, acc[0], 1, TPI);
+      if (lane == TPI - 1) nxt = 0u;
+#pragma unroll
+      for (int j = 0; j <= L; ++j) acc[j] = acc[j + 1];
+      acc[L + 1] = 0u;
+      ptx::add_cc(acc[L - 1], acc[L - 1], nxt);
+      ptx::addc_cc(acc[L], acc[L], 0u);
+      ptx::addc(acc[L + 1], acc[L + 1], 0u);
+    }
+#pragma unroll
+    for (int round = 1; round < TPI; ++round) {
+      uint32_t o0 = __shfl_up_sync(mask, acc[L], 1, TPI);
+      uint32_t o1 = __shfl_up_sync(mask, acc[L + 1], 1, TPI);
+      if (lane == 0) o0 = o1 = 0u;
+      acc[L] = 0u;
+      acc[L + 1] = 0u;
+      ptx::add_cc(acc[0], acc[0], o0);
+      ptx::addc_cc(acc[1], acc[1], o1);
+#pragma unroll
+      for (int j = 2; j < L + 1; ++j) ptx::addc_cc(acc[j], acc[j], 0u);
+      ptx::addc(acc[L + 1], acc[L + 1], 0u);
+    }
+#pragma unroll
+    for (int j = 0; j < L; ++j) r[j] = acc[j];
+  }
+};
+
+template <class P, int TPI>
+__global__ void coop_chain_kernel(uint32_t* sink, int iters) {
+  using C = Coop<P, TPI>;
+  const int lane = threadIdx.x % TPI;
+  const unsigned mask = 0xFFFFFFFFu;
+  uint32_t pl[C::L], x1[C::L], x2[C::L], y[P::N];
+  C::load_mod(pl, lane);
+#pragma unroll
+  for (int j = 0; j < C::L; ++j) {
+    x1[j] = (threadIdx.x / TPI + 1) * 0x9E3779B9u + j + lane;
+    x2[j] = (blockIdx.x + 7) * 0x85EBCA6Bu + 3 * j + lane;
+  }
+  if (lane == TPI - 1) {
+    x1[C::L - 1] &= 0xFFFFu;
+    x2[C::L - 1] &= 0xFFFFu;
+  }
+#pragma unroll
+  for (int j = 0; j < P::N; ++j) y[j] = 0xC2B2AE35u * (j + 11) + (blockIdx.x ^ (threadIdx.x / TPI));
+  y[P::N - 1] &= 0xFFFFu;
+  for (int it = 0; it < iters; ++it) {
+    C::mul(x1, x1, y, pl, lane, mask);
+    C::mul(x2, x2, y, pl, lane, mask);
+  }
+  uint32_t acc = 0;
+#pragma unroll
+  for (int j = 0; j < C::L; ++j) acc ^= x1[j] ^ (x2[j] * (j + 1));
+  sink[blockIdx.x * blockDim.x + threadIdx.x] = acc;
+}
+
+// One cooperative product per group on given operands (a: N limbs per group,
+// b: N limbs per group), result (N limbs, in [0, 2p)) per group.
+template <class P, int TPI>
+__global__ void coop_check_kernel(const uint32_t* a, const uint32_t* b, uint32_t* out, int groups) {
+  using C = Coop<P, TPI>;
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) / TPI;
+  const int lane = threadIdx.x % TPI;
+  if ((blockIdx.x * blockDim.x) / TPI >= groups) return;  // whole-warp exit only
+  const int gg = g < groups ? g : groups - 1;
+  uint32_t pl[C::L], x[C::L], bb[P::N], r[C::L];
+  C::load_mod(pl, lane);
+#pragma unroll
+  for (int j = 0; j < C::L; ++j) x[j] = a[(uint64_t)gg * P::N + lane * C::L + j];
+#pragma unroll
+  for (int j = 0; j < P::N; ++j) bb[j] = b[(uint64_t)gg * P::N + j];
+  C::mul(r, x, bb, pl, lane, 0xFFFFFFFFu);
+  if (g < groups)
+#pragma unroll
+    for (int j = 0; j < C::L; ++j) out[(uint64_t)g * P::N + lane * C::L + j] = r[j];
+}
+
+template <class P, int TPI>
+static int run_coop_bench(int iters, double* muls_per_s) {
+  // correctness first: 256 products against the host arithmetic (mod p)
+  const int groups = 256;
+  std::vector<uint32_t> ha((size_t)groups * P::N), hb((size_t)groups * P::N), ho((size_t)groups * P::N);
+  uint64_t s = 0x5EEDC00Full;
+  for (size_t i = 0; i < ha.size(); ++i) {
+    s = s * 6364136223846793005ull + 1442695040888963407ull;
+    ha[i] = (uint32_t)(s >> 32);
+    s = s * 6364136223846793005ull + 1442695040888963407ull;
+    hb[i] = (uint32_t)(s >> 32);
+  }
+  for (int g = 0; g < groups; ++g) {
+    ha[(size_t)g * P::N + P::N - 1] &= 0xFFFFu;
+    hb[(size_t)g * P::N + P::N - 1] &= 0xFFFFu;
+  }
+  uint32_t *da = nullptr, *db = nullptr, *dout = nullptr;
+  int rc = dev_alloc((void**)&da, ha.size() * 4);
+  if (!rc) rc = dev_alloc((void**)&db, hb.size() * 4);
+  if (!rc) rc = dev_alloc((void**)&dout, ho.size() * 4);
+  if (rc) {
+    dev_free(da);
+    dev_free(db);
+    return rc;
+  }
+  cudaMemcpy(da, ha.data(), ha.size() * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(db, hb.data(), hb.size() * 4, cudaMemcpyHostToDevice);
+  coop_check_kernel<P, TPI><<<(groups * TPI + 127) / 128, 128>>>(da, db, dout, groups);
+  cudaError_t err = cudaMemcpy(ho.data(), dout, ho.size() * 4, cudaMemcpyDeviceToHost);
+  dev_free(da);
+  dev_free(db);
+  dev_free(dout);
+  count_launches(1);
+  if (err != cudaSuccess) return cuda_fail(err, "cooperative product check");
+  for (int g = 0; g < groups; ++g) {
+    HFe<P> x, y, z;
+    std::memcpy(x.l, &ha[(size_t)g * P::N], sizeof(x.l));
+    std::memcpy(y.l, &hb[(size_t)g * P::N], sizeof(y.l));
+    // reduce the operands (they may exceed p), then compare a*b*R^-1 mod p
+    HFe<P> one = h_small<P>(1);
+    HFe<P> xr = h_mont_mul<P>(h_mont_mul<P>(x, h_r2<P>()), one);
+    HFe<P> yr = h_mont_mul<P>(h_mont_mul<P>(y, h_r2<P>()), one);
+    HFe<P> want = h_mont_mul<P>(xr, yr);
+    std::memcpy(z.l, &ho[(size_t)g * P::N], sizeof(z.l));
+    HFe<P> got = h_mont_mul<P>(h_mont_mul<P>(z, h_r2<P>()), one);  // z mod p
+    if (!h_eq<P>(got, want)) return set_error(GSN_ERR_STATE, "cooperative product mismatch at group %d", g);
+  }
+  int dev = 0, sms = 0, per_sm = 0;
+  GSN_CUDA(cudaGetDevice(&dev));
+  GSN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int block = 128;
+  GSN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, coop_chain_kernel<P, TPI>, block, 0));
+  const int grid = sms * std::max(per_sm, 1);
+  uint32_t* sink = nullptr;
+  rc = dev_alloc((void**)&sink, (size_t)grid * block * sizeof(uint32_t));
+  if (rc) return rc;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  coop_chain_kernel<P, TPI><<<grid, block>>>(sink, iters / 8 + 1);
+  cudaEventRecord(e0);
+  coop_chain_kernel<P, TPI><<<grid, block>>>(sink, iters);
+  cudaEventRecord(e1);
+  err = cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  dev_free(sink);
+  count_launches(2);
+  if (err != cudaSuccess) return cuda_fail(err, "cooperative product benchmark");
+  *muls_per_s = 2.0 * (grid * block / TPI) * (double)iters / (ms * 1e-3);
+  return GSN_OK;
+}
+
 }  // namespace gsn
 
 using namespace gsn;
+
+/* lanes = 1: the per-thread schedules (schedule 0/1); lanes = 2 or 4: the
+ * cooperative product (MNT4-753 only). */
+extern "C" int gsn_microbench_mont_coop(int field, int lanes, int iters, double* muls_per_s) {
+  if (iters <= 0 || !muls_per_s) return set_error(GSN_ERR_ARG, "bad microbenchmark arguments");
+  if (field != GSN_MNT4753_FR) return set_error(GSN_ERR_FIELD, "cooperative product is built for MNT4-753");
+  if (lanes == 2) return run_coop_bench<FieldMNT4_753, 2>(iters, muls_per_s);
+  if (lanes == 4) return run_coop_bench<FieldMNT4_753, 4>(iters, muls_per_s);
+  return set_error(GSN_ERR_ARG, "lanes must be 2 or 4");
+}
 
 extern "C" int gsn_microbench_mont(int field, int schedule, int iters, double* muls_per_s) {
   if (iters <= 0 || !muls_per_s || (schedule != 0 && schedule != 1))

@@ -262,6 +262,10 @@ int gsn_microbench_imad(int iters, double* mads_per_s, double* mads_per_clk_sm, 
 /* Throughput (products per second, all SMs) of the multi-limb Montgomery
  * product with schedule 0 (row chains) or 1 (even/odd accumulators). */
 int gsn_microbench_mont(int field, int schedule, int iters, double* muls_per_s);
+/* Same for the cooperative MNT4-753 product split over `lanes` (2 or 4)
+ * threads per element; checks 256 products against the host arithmetic
+ * first (GSN_ERR_STATE on a mismatch). */
+int gsn_microbench_mont_coop(int field, int lanes, int iters, double* muls_per_s);
 
 #ifdef __cplusplus
 }
