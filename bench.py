@@ -5,8 +5,9 @@ Headline workload (``value``): forward NTT over the MNT4-753 scalar field r
 the input (25 MB) is smaller than L2, so L2 is flushed (256 MB write) before
 every timed step and only the transform is timed, with CUDA events on the
 launching stream.  ``e2e`` is the same transform through the C-ABI host entry
-point gsn_ntt_host (the best_fft drop-in) from pinned host memory, copies
-included.  ``roofline`` compares the transform's algorithmic integer
+point gsn_ntt_host (the best_fft drop-in) on a pinned host buffer: the input
+is copied in from and the result copied back to host memory inside the timed
+region.  ``roofline`` compares the transform's algorithmic integer
 multiply-adds (2352 per 24-limb Montgomery product, (n/2) log2 n products)
 with the measured throughput of the same PTX carry-chain instructions
 (gsn_microbench_imad) in the same process.
@@ -143,6 +144,26 @@ def imad_peak(g) -> dict:
     a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
     g._lib.check(lib.gsn_microbench_imad(20000, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
     return {"mads_per_s": a.value, "mads_per_clk_sm": b.value, "sm_mhz": c.value}
+
+
+def montgomery_schedules(g, iters: int = 2000) -> dict:
+    """Montgomery products per second on the whole GPU for the one-thread schedules (0 row chains,
+    1 even/odd accumulators) and the 24-limb product split over 2 or 4 cooperating lanes."""
+    lib = g.load()
+    out = {}
+    for name, fid in (("bls12_381_fr", 1), ("mnt4753_fr", 2)):
+        per = {}
+        for sched in (0, 1):
+            v = ctypes.c_double()
+            g._lib.check(lib.gsn_microbench_mont(fid, sched, iters, ctypes.byref(v)))
+            per[f"thread_schedule{sched}_G_per_s"] = round(v.value / 1e9, 3)
+        if fid == 2:
+            for lanes in (2, 4):
+                v = ctypes.c_double()
+                g._lib.check(lib.gsn_microbench_mont_coop(fid, lanes, iters, ctypes.byref(v)))
+                per[f"coop_{lanes}_lanes_G_per_s"] = round(v.value / 1e9, 3)
+        out[name] = per
+    return out
 
 
 def time_device_ntt(g, torch, f, log_n: int, steps: int, warmup: int, direction=0, flush=None):
@@ -310,7 +331,8 @@ def run_gpu(args, rank, local, ws):
                    "l2": "flushed (256 MB write) before each step; input 25 MB < L2",
                    "parallelism": f"replicas x{ws}"},
         "e2e": {"value": round(n * ws / e2e_t / 1e6, 3), "unit": "Melem/s", "h2d_bytes_per_step": nbytes,
-                "d2h_bytes_per_step": nbytes, "api": "gsn_ntt_host (pinned host buffer)"},
+                "d2h_bytes_per_step": nbytes,
+                "api": "gsn_ntt_host on a pinned host buffer (copy in, transform, copy out)"},
         "roofline": {"bound": "imad", "achieved": round(achieved / 1e12, 4),
                      "peak": round(ip["mads_per_s"] / 1e12, 4), "unit": "TIMAD/s",
                      "frac": round(achieved / ip["mads_per_s"], 4), "traffic": None,
@@ -347,6 +369,7 @@ def run_gpu(args, rank, local, ws):
         except Exception as exc:
             extra["serving"] = {"error": str(exc)}
         extra["imad_microbench"] = ip
+        extra["montgomery_schedules"] = montgomery_schedules(g)
         line["extra"] = extra
     return line
 

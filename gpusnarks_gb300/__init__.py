@@ -121,6 +121,25 @@ def pointwise_mul(field, a, b, *, stream=None):
     return a
 
 
+def coset_quotient(field, a, b, c, *, shift=None, stream=None):
+    """In place on device tensors of coset evaluations: a = (a*b - c) / (shift^n - 1)."""
+    f = field_of(field)
+    log_n = _log2_exact(a.numel() // f.limbs)
+    check(load().gsn_coset_quotient(f.fid, a.data_ptr(), b.data_ptr(), c.data_ptr(), log_n,
+                                    u32p(_limbs(f, shift)), _stream_handle(stream)))
+    return a
+
+
+def qap_h(field, a, b, c, *, shift=None, stream=None):
+    """H = (A*B - C) / Z from the evaluations of A, B, C on the domain (device tensors); the n
+    coefficients of H land in ``a``; ``b`` and ``c`` are overwritten."""
+    f = field_of(field)
+    log_n = _log2_exact(a.numel() // f.limbs)
+    check(load().gsn_qap_h(f.fid, a.data_ptr(), b.data_ptr(), c.data_ptr(), log_n, u32p(_limbs(f, shift)),
+                           _stream_handle(stream)))
+    return a
+
+
 TO_MONTGOMERY, FROM_MONTGOMERY, REVERSE_LIMBS = 0, 1, 2
 
 
@@ -182,3 +201,4 @@ def host_buffer(nbytes: int):
 
 def free_host_buffer(p) -> None:
     check(load().gsn_host_free(p))
+

@@ -45,6 +45,10 @@ _SIGNATURES = [
     ("gsn_prepare", ctypes.c_int, [ctypes.c_int, ctypes.c_uint32, _u32p]),
     ("gsn_pointwise_mul", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
                                          ctypes.c_void_p]),
+    ("gsn_coset_quotient", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_uint32, _u32p, ctypes.c_void_p]),
+    ("gsn_qap_h", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
+                                 _u32p, ctypes.c_void_p]),
     ("gsn_convert", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p]),
     ("gsn_synchronize", ctypes.c_int, [ctypes.c_void_p]),
     ("gsn_host_alloc", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]),
@@ -57,6 +61,7 @@ _SIGNATURES = [
                                            ctypes.POINTER(ctypes.c_double)]),
     ("gsn_microbench_mont_coop", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                                 ctypes.POINTER(ctypes.c_double)]),
+    ("gsn_microbench_p32_butterfly", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     ("gsn_batch_create", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int,
                                         ctypes.POINTER(ctypes.c_void_p)]),
     ("gsn_batch_launch", ctypes.c_int, [ctypes.c_void_p, ctypes.c_void_p]),

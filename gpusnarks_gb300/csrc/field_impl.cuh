@@ -47,6 +47,7 @@ constexpr FieldOps make_field_ops(int max_log_n, int default_tw_log) {
                   &Kernels<P>::pass,
                   &Kernels<P>::powers,
                   &Kernels<P>::pointwise,
+                  &Kernels<P>::quotient,
                   &Kernels<P>::fill,
                   &Kernels<P>::convert,
                   &Kernels<P>::batch,

@@ -20,6 +20,9 @@ struct FieldOps {
   cudaError_t (*pass)(const PassArgs& A, int block, cudaStream_t s);
   cudaError_t (*powers)(uint32_t* out, uint64_t count, const uint32_t* base_canon, cudaStream_t s);
   cudaError_t (*pointwise)(uint32_t* a, const uint32_t* b, uint64_t n, cudaStream_t s);
+  // a[i] = (a[i] b[i] - c[i]) z, zr2 = z R^2 (limbs)
+  cudaError_t (*quotient)(uint32_t* a, const uint32_t* b, const uint32_t* c, uint64_t n, const uint32_t* zr2,
+                          cudaStream_t s);
   cudaError_t (*fill)(uint32_t* out, uint64_t n, uint64_t seed, cudaStream_t s);
   cudaError_t (*convert)(uint32_t* data, uint64_t n, int mode, cudaStream_t s);
   cudaError_t (*batch)(const BatchJob* jobs_dev, const uint64_t* work_dev, uint64_t nwork,

@@ -84,6 +84,7 @@ struct P32Args {
   int has_pre_const;
   int lo_bits;
   int log_n, log_r, log_inner, log_outer, log_j, last, first, npass;
+  int pipe;                    // set by the launcher: non-last pass with two tile buffers (prefetch)
   int radix_log[kMaxPasses];
 };
 

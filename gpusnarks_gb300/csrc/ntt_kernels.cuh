@@ -300,6 +300,29 @@ __global__ void pointwise_mul_kernel(uint32_t* a, const uint32_t* b, uint64_t n)
   }
 }
 
+// Coset quotient of the QAP witness map: a[i] = (a[i] * b[i] - c[i]) * z, with
+// z = 1 / Z(shift * w^i) = 1 / (shift^n - 1) the same for every point of a
+// radix-2 coset.  Inputs canonical; zr2 = z * R^2 (Montgomery, twice), so
+//   (mont(a, b) - mont(c, 1)) = (a b - c) / R  and  mont(that, z R^2) = (a b - c) z.
+template <class P>
+__global__ void coset_quotient_kernel(uint32_t* a, const uint32_t* b, const uint32_t* c, uint64_t n, Fe<P> zr2) {
+  Fe<P> one;
+#pragma unroll
+  for (int j = 0; j < P::N; ++j) one.l[j] = j == 0 ? 1u : 0u;
+  for (uint64_t i = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    Fe<P> x, y, z, t, u;
+    fe_load<P>(x, a + i * P::N);
+    fe_load<P>(y, b + i * P::N);
+    fe_load<P>(z, c + i * P::N);
+    fe_mul<P>(t, x, y);
+    fe_mul<P>(u, z, one);
+    fe_sub<P>(t, t, u);
+    fe_mul<P>(t, t, zr2);
+    fe_store<P>(a + i * P::N, t);
+  }
+}
+
 // ---------------------------------------------------------------------------
 // Batched transforms: one persistent launch over many jobs.
 //
@@ -451,6 +474,17 @@ struct Kernels {
     uint64_t grid = (n + block - 1) / block;
     if (grid > 152 * 64) grid = 152 * 64;
     pointwise_mul_kernel<P><<<(unsigned)grid, block, 0, s>>>(a, b, n);
+    return cudaGetLastError();
+  }
+  static cudaError_t quotient(uint32_t* a, const uint32_t* b, const uint32_t* c, uint64_t n, const uint32_t* zr2,
+                              cudaStream_t s) {
+    Fe<P> z;
+    for (int i = 0; i < P::N; ++i) z.l[i] = zr2[i];
+    const int block = 256;
+    uint64_t grid = (n + block - 1) / block;
+    if (grid > 152 * 64) grid = 152 * 64;
+    if (grid == 0) return cudaSuccess;
+    coset_quotient_kernel<P><<<(unsigned)grid, block, 0, s>>>(a, b, c, n, z);
     return cudaGetLastError();
   }
 };

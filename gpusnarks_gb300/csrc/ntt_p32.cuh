@@ -76,6 +76,21 @@ __device__ __forceinline__ uint4 mul4v(uint4 a, uint4 w) {
   return make_uint4(mm(a.x, w.x), mm(a.y, w.y), mm(a.z, w.z), mm(a.w, w.w));
 }
 
+// DIF butterfly of the last stage, whose twiddle is w^0 = 1: (a, b) -> (a + b, a - b)
+__device__ __forceinline__ void bfly4_unit(uint4& a, uint4& b) {
+  uint4 s, d;
+  s.x = add1<F>(a.x, b.x);
+  d.x = sub1<F>(a.x, b.x);
+  s.y = add1<F>(a.y, b.y);
+  d.y = sub1<F>(a.y, b.y);
+  s.z = add1<F>(a.z, b.z);
+  d.z = sub1<F>(a.z, b.z);
+  s.w = add1<F>(a.w, b.w);
+  d.w = sub1<F>(a.w, b.w);
+  a = s;
+  b = d;
+}
+
 // DIF butterfly on 4 columns: (a, b) -> (a + b, (a - b) * w)
 __device__ __forceinline__ void bfly4(uint4& a, uint4& b, uint32_t w) {
   uint4 s, d;
@@ -272,7 +287,7 @@ __host__ __device__ constexpr uint32_t chunk_c(uint32_t row) {
   return (row << LCG) ^ ((x & ((1u << SH) - 1u)) << LCG);
 }
 
-template <int ET, int LS, int S0, int LCG>
+template <int ET, int LS, int S0, int LCG, int RL>
 __device__ __forceinline__ void substep_fixed(uint4* sm, const uint32_t* __restrict__ twt, uint32_t base_chunk,
                                               uint32_t low) {
   constexpr int E = 1 << ET;
@@ -281,6 +296,11 @@ __device__ __forceinline__ void substep_fixed(uint4* sm, const uint32_t* __restr
   for (int m = 0; m < E; ++m) x[m] = sm[base_chunk ^ chunk_c<LCG>((uint32_t)m << LS)];
 #pragma unroll
   for (int q = 0; q < ET; ++q) {
+    if (S0 + q == RL - 1) {  // last stage of the pass: LS = 0, t = 0, low = 0, twiddle w^0 = 1
+#pragma unroll
+      for (int g = 0; g < (E >> 1); ++g) bfly4_unit(x[2 * g], x[2 * g + 1]);
+      continue;
+    }
     const uint32_t* tq = twt + (low << (S0 + q));
 #pragma unroll
     for (int t = 0; t < (E >> (q + 1)); ++t) {
@@ -307,14 +327,115 @@ __device__ __forceinline__ void substeps_fixed(uint4* sm, const uint32_t* __rest
       const uint32_t uu = u >> LCG;
       const uint32_t low = uu & ((1u << ls) - 1u);
       const uint32_t rowbase = ((uu >> ls) << (RL - S0)) | low;
-      substep_fixed<et, ls, S0, LCG>(sm, twt, chunk_c<LCG>(rowbase) ^ cg, low);
+      substep_fixed<et, ls, S0, LCG, RL>(sm, twt, chunk_c<LCG>(rowbase) ^ cg, low);
     }
     __syncthreads();
     substeps_fixed<RL, ET, LCG, S0 + et>(sm, twt);
   }
 }
 
+// Column tile of a non-last pass: base offset of its first element, first column.
+template <int RL, int LCG>
+__device__ __forceinline__ void column_tile(const P32Args& A, uint64_t tile, uint64_t& base, uint64_t& jbase) {
+  constexpr int lj = LCG + 2;
+  const int per_prefix_log = A.log_inner - lj;
+  const uint64_t prefix = tile >> per_prefix_log;
+  jbase = (tile & (((uint64_t)1 << per_prefix_log) - 1)) << lj;
+  base = (prefix << (RL + A.log_inner)) + jbase;
+}
+
+// Asynchronous global -> shared copy of a column tile into the swizzled layout (cp.async, 16 bytes per
+// chunk: base and 2^log_inner are multiples of 4 elements and the array is 16-byte aligned).
+template <int RL, int LCG>
+__device__ __forceinline__ void prefetch_columns(const P32Args& A, uint4* buf, uint64_t base) {
+  constexpr uint32_t CG = 1u << LCG, R = 1u << RL;
+  const uint32_t sb = (uint32_t)__cvta_generic_to_shared(buf);
+  for (uint32_t v = threadIdx.x; v < R * CG; v += blockDim.x) {
+    const uint32_t k = v >> LCG, cg = v & (CG - 1);
+    const uint32_t* g = A.src + base + ((uint64_t)k << A.log_inner) + 4 * cg;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(sb + 16u * chunk_of<LCG>(k, cg)), "l"(g)
+                 : "memory");
+  }
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
+
+// Four-step twiddle W_c(k) = w_n^((jp + c) k 2^outer) and store of a finished column tile (rows in
+// bit-reversed order in shared memory).  The thread visits rows k0, k0 + dk, ... (blockDim is a
+// multiple of CG, so its column group is fixed), so W advances by one product with W_c(dk) per row.
+template <int RL, int LCG>
+__device__ __forceinline__ void store_fourstep(const P32Args& A, const uint4* sm, uint64_t base, uint64_t jbase) {
+  constexpr uint32_t CG = 1u << LCG, R = 1u << RL;
+  const uint32_t cg = threadIdx.x & (CG - 1);
+  const uint32_t k0 = threadIdx.x >> LCG, dk = blockDim.x >> LCG;
+  if (k0 >= R) return;
+  const uint64_t e0 = (jbase + 4 * cg) << A.log_outer, e1 = e0 + (1ull << A.log_outer),
+                 e2 = e1 + (1ull << A.log_outer), e3 = e2 + (1ull << A.log_outer);
+  uint4 w = make_uint4(tw_n(A, e0 * k0), tw_n(A, e1 * k0), tw_n(A, e2 * k0), tw_n(A, e3 * k0));
+  uint4 st = make_uint4(0u, 0u, 0u, 0u);
+  if (k0 + dk < R) st = make_uint4(tw_n(A, e0 * dk), tw_n(A, e1 * dk), tw_n(A, e2 * dk), tw_n(A, e3 * dk));
+  for (uint32_t k = k0; k < R; k += dk) {
+    uint4 x = sm[chunk_of<LCG>(brev(k, RL), cg)];
+    x = mul4v(x, w);
+    *reinterpret_cast<uint4*>(A.dst + base + ((uint64_t)k << A.log_inner) + 4 * cg) = x;
+    if (k + dk < R) w = mul4v(w, st);
+  }
+}
+
 }  // namespace p32
+
+// Non-last pass with two tile buffers (A.pipe): while one tile is transformed, the next tile of this CTA
+// streams into the other buffer with cp.async.  The trailing __syncthreads of an iteration ends all reads
+// of the buffer the next iteration starts filling.  Same arithmetic and results as ntt_p32_fixed_kernel.
+template <int RL, int ET, int LCG>
+__global__ void __launch_bounds__(512) ntt_p32_pipe_kernel(P32Args A) {
+  using namespace p32;
+  extern __shared__ uint4 gsn_smem[];
+  constexpr uint32_t CG = 1u << LCG;
+  constexpr uint32_t R = 1u << RL;
+  {
+    uint4* const buf0 = gsn_smem;
+    uint4* const buf1 = gsn_smem + R * CG;
+    uint64_t tile = blockIdx.x, base = 0, jbase = 0;
+    if (tile < A.tiles) {
+      column_tile<RL, LCG>(A, tile, base, jbase);
+      prefetch_columns<RL, LCG>(A, buf0, base);
+    }
+    cp_async_commit();
+    bool odd = false;
+    for (; tile < A.tiles; tile += gridDim.x) {
+      uint4* const cur = odd ? buf1 : buf0;
+      const uint64_t next = tile + gridDim.x;
+      uint64_t nbase = 0, njbase = 0;
+      if (next < A.tiles) {
+        column_tile<RL, LCG>(A, next, nbase, njbase);
+        prefetch_columns<RL, LCG>(A, odd ? buf0 : buf1, nbase);
+      }
+      cp_async_commit();
+      cp_async_wait<1>();  // this tile's copies (all but the group just committed) have landed
+      __syncthreads();
+      if (A.first && (A.pre_table || A.has_pre_const)) {
+        for (uint32_t v = threadIdx.x; v < R * CG; v += blockDim.x) {
+          const uint32_t k = v >> LCG, cg = v & (CG - 1);
+          const uint64_t g = base + ((uint64_t)k << A.log_inner) + 4 * cg;
+          sm_st<LCG>(cur, k, cg, premul(A, sm_ld<LCG>(cur, k, cg), g));
+        }
+        __syncthreads();
+      }
+      substeps_fixed<RL, ET, LCG, 0>(cur, A.tw_tile);  // ends with __syncthreads()
+      store_fourstep<RL, LCG>(A, cur, base, jbase);
+      __syncthreads();
+      base = nbase;
+      jbase = njbase;
+      odd = !odd;
+    }
+    cp_async_wait<0>();
+  }
+}
 
 template <int RL, int ET, int LCG>
 __global__ void __launch_bounds__(512) ntt_p32_fixed_kernel(P32Args A) {
@@ -372,20 +493,12 @@ __global__ void __launch_bounds__(512) ntt_p32_fixed_kernel(P32Args A) {
 
     substeps_fixed<RL, ET, LCG, 0>(sm, A.tw_tile);  // ends with __syncthreads()
 
-    for (uint32_t v = threadIdx.x; v < R * CG; v += blockDim.x) {
-      const uint32_t k = v >> LCG, cg = v & (CG - 1);
-      uint4 x = sm_ld<LCG>(sm, brev(k, RL), cg);
-      if (!A.last) {
-        const uint64_t jp = jbase + 4 * cg;
-        const uint64_t ek = (uint64_t)k << A.log_outer;
-        uint4 w;
-        w.x = tw_n(A, jp * ek);
-        w.y = tw_n(A, (jp + 1) * ek);
-        w.z = tw_n(A, (jp + 2) * ek);
-        w.w = tw_n(A, (jp + 3) * ek);
-        x = mul4v(x, w);
-        *reinterpret_cast<uint4*>(A.dst + base + ((uint64_t)k << A.log_inner) + 4 * cg) = x;
-      } else {
+    if (!A.last) {
+      store_fourstep<RL, LCG>(A, sm, base, jbase);
+    } else {
+      for (uint32_t v = threadIdx.x; v < R * CG; v += blockDim.x) {
+        const uint32_t k = v >> LCG, cg = v & (CG - 1);
+        uint4 x = sm_ld<LCG>(sm, brev(k, RL), cg);
         const uint64_t opos = obase + 4 * cg + ((uint64_t)k << A.log_outer);
         if (A.post_table) x = mul4v(x, __ldg(reinterpret_cast<const uint4*>(A.post_table + opos)));
         *reinterpret_cast<uint4*>(A.dst + opos) = x;
@@ -404,21 +517,40 @@ cudaError_t p32_launch_et(const P32Args& A, int block, int grid_cap, cudaStream_
 
 #ifdef GSN_P32_INSTANTIATE_ET
 namespace p32 {
+// Tiles up to this size get a second buffer on non-last passes of the fixed-radix kernel (prefetch of
+// the CTA's next tile), keeping at least two CTAs' worth of shared memory per SM.
+constexpr size_t kPipeTileMax = 48 * 1024;
+
 template <class K>
-cudaError_t launch_kernel(K k, const P32Args& A, int block, int grid_cap, cudaStream_t s) {
-  const size_t smem = ((size_t)1 << (A.log_r + A.log_j)) * sizeof(uint32_t);
+cudaError_t launch_kernel(K k, const P32Args& A, int block, int grid_cap, cudaStream_t s, bool pipe = false) {
+  P32Args B = A;
+  B.pipe = pipe ? 1 : 0;
+  const size_t tile = ((size_t)1 << (A.log_r + A.log_j)) * sizeof(uint32_t);
+  const size_t smem = pipe ? 2 * tile : tile;
   if (smem > kDefaultSmemOptIn) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
   }
   const uint64_t grid = A.tiles < (uint64_t)grid_cap ? A.tiles : (uint64_t)grid_cap;
-  k<<<(unsigned)grid, block, smem, s>>>(A);
+  k<<<(unsigned)grid, block, smem, s>>>(B);
   return cudaGetLastError();
+}
+inline bool pipe_enabled() {
+  static const int on = [] {
+    const char* e = getenv("GSN_P32_PIPE");
+    return e ? atoi(e) : 1;
+  }();
+  return on != 0;
 }
 template <int ET, int LCG, int RL>
 cudaError_t launch_fixed(const P32Args& A, int block, int grid_cap, cudaStream_t s) {
   if constexpr (RL <= 13) {
-    if (A.log_r == RL) return launch_kernel(ntt_p32_fixed_kernel<RL, ET, LCG>, A, block, grid_cap, s);
+    if (A.log_r == RL) {
+      const size_t tile = ((size_t)1 << (A.log_r + A.log_j)) * sizeof(uint32_t);
+      if (!A.last && tile <= kPipeTileMax && pipe_enabled())
+        return launch_kernel(ntt_p32_pipe_kernel<RL, ET, LCG>, A, block, grid_cap, s, true);
+      return launch_kernel(ntt_p32_fixed_kernel<RL, ET, LCG>, A, block, grid_cap, s);
+    }
     return launch_fixed<ET, LCG, RL + 1>(A, block, grid_cap, s);
   } else {
     return launch_kernel(ntt_p32_kernel<ET, LCG>, A, block, grid_cap, s);

@@ -503,7 +503,17 @@ static int ntt_impl(int field, uint32_t* data, uint32_t log_n, const uint32_t* o
   Tables T;
   rc = resolve_tables(*F, log_n, omega, dir, shift, &T, s);
   if (rc) return rc;
+  if (scratch) {
+    rc = check_data_ptr(*F, scratch);
+    if (rc) return rc;
+  }
   Plan plan = plan_for(*F, (int)log_n);
+  if (plan.kernel == kKernelP32 &&
+      (reinterpret_cast<uintptr_t>(data) % 16 || reinterpret_cast<uintptr_t>(scratch) % 16)) {
+    // the register-blocked 32-bit pass moves 16-byte vectors; 4-byte-aligned arrays take the generic pass
+    const FieldLimits L = limits_of(*F);
+    plan = make_plan(*F, (int)log_n, L.max_r, L.target_j, L.max_block);
+  }
   if (plan.kernel == kKernelP32) {
     rc = resolve_p32_tables(*F, plan, &T);
     if (rc) return rc;
@@ -515,8 +525,51 @@ static int ntt_impl(int field, uint32_t* data, uint32_t log_n, const uint32_t* o
   return enqueue_ntt(*F, plan, T, data, scratch, s);
 }
 
-static std::mutex g_host_mu;
+// zr2 = z * R^2 with z = 1 / Z(shift * w^i) = 1 / (shift^n - 1), the inverse vanishing polynomial of the
+// size-n radix-2 domain on its coset by `shift` (null: the field's generator).
+static int coset_z_inv(const FieldOps& F, uint32_t log_n, const uint32_t* shift, uint32_t* zr2) {
+  uint32_t s[kMaxLimbs] = {0}, t[kMaxLimbs] = {0}, u[kMaxLimbs] = {0};
+  if (shift) {
+    if (!F.is_canonical(shift)) return set_error(GSN_ERR_ARG, "shift is not a canonical field element");
+    std::memcpy(s, shift, F.limbs * sizeof(uint32_t));
+  } else {
+    s[0] = F.generator;
+  }
+  bool zero = true;
+  for (int i = 0; i < F.limbs; ++i) zero = zero && s[i] == 0;
+  if (zero) return set_error(GSN_ERR_ARG, "shift must be nonzero");
+  F.pow(s, (uint64_t)1 << log_n, t);
+  bool one = t[0] == 1;
+  for (int i = 1; i < F.limbs; ++i) one = one && t[i] == 0;
+  if (one) return set_error(GSN_ERR_ARG, "shift^n = 1: Z(x) = x^n - 1 vanishes on that coset");
+  for (int i = 0; i < F.limbs; ++i) {  // t - 1; t >= 2 here
+    if (t[i]--) break;
+  }
+  F.inv(t, u);
+  F.to_mont(u, t);
+  F.to_mont(t, zr2);
+  return GSN_OK;
+}
 
+static int quotient_impl(int field, uint32_t* a, const uint32_t* b, const uint32_t* c, uint32_t log_n,
+                         const uint32_t* shift, cudaStream_t s) {
+  const FieldOps* F = field_ops(field);
+  if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);
+  if ((int)log_n > F->two_adicity) return set_error(GSN_ERR_SIZE, "log_n=%u exceeds the 2-adicity", log_n);
+  int rc = check_data_ptr(*F, a);
+  if (!rc) rc = check_data_ptr(*F, b);
+  if (!rc) rc = check_data_ptr(*F, c);
+  if (rc) return rc;
+  uint32_t zr2[kMaxLimbs];
+  rc = coset_z_inv(*F, log_n, shift, zr2);
+  if (rc) return rc;
+  cudaError_t e = F->quotient(a, b, c, (uint64_t)1 << log_n, zr2, s);
+  if (e != cudaSuccess) return cuda_fail(e, "coset quotient launch");
+  count_launches(1);
+  return GSN_OK;
+}
+
+static std::mutex g_host_mu;
 }  // namespace gsn
 
 using namespace gsn;
@@ -621,6 +674,26 @@ int gsn_pointwise_mul(int field, uint32_t* a, const uint32_t* b, uint64_t n, voi
   if (e != cudaSuccess) return cuda_fail(e, "pointwise multiply launch");
   count_launches(1);
   return GSN_OK;
+}
+
+int gsn_coset_quotient(int field, uint32_t* a, const uint32_t* b, const uint32_t* c, uint32_t log_n,
+                       const uint32_t* shift, void* stream) {
+  return quotient_impl(field, a, b, c, log_n, shift, static_cast<cudaStream_t>(stream));
+}
+
+int gsn_qap_h(int field, uint32_t* a, uint32_t* b, uint32_t* c, uint32_t log_n, const uint32_t* shift,
+              void* stream) {
+  if (a == b || a == c || b == c) return set_error(GSN_ERR_ARG, "a, b and c must be distinct arrays");
+  const cudaStream_t s = static_cast<cudaStream_t>(stream);
+  uint32_t* polys[3] = {a, b, c};
+  for (uint32_t* x : polys) {  // evaluations on the domain -> coefficients -> evaluations on the coset
+    int rc = ntt_impl(field, x, log_n, nullptr, GSN_INVERSE, nullptr, nullptr, s);
+    if (!rc) rc = ntt_impl(field, x, log_n, nullptr, GSN_COSET_FORWARD, shift, nullptr, s);
+    if (rc) return rc;
+  }
+  int rc = quotient_impl(field, a, b, c, log_n, shift, s);
+  if (rc) return rc;
+  return ntt_impl(field, a, log_n, nullptr, GSN_COSET_INVERSE, shift, nullptr, s);
 }
 
 int gsn_convert(int field, uint32_t* data, uint64_t n, int mode, void* stream) {

@@ -114,6 +114,26 @@ int gsn_prepare(int field, uint32_t log_n, const uint32_t* omega);
 /* a[i] = a[i] * b[i] mod p on device memory (canonical values). */
 int gsn_pointwise_mul(int field, uint32_t* a, const uint32_t* b, uint64_t n, void* stream);
 
+/* Polynomial step after the NTT in a QAP (Groth16-style) prover; no
+ * counterpart in the reference, which stops at the FFT.  For evaluations
+ * a, b, c of A, B, C on the coset shift*<w> of the size-n = 2^log_n domain:
+ *   a[i] = (a[i] * b[i] - c[i]) / Z(shift * w^i),   Z(x) = x^n - 1,
+ * i.e. times 1/(shift^n - 1).  shift = NULL selects the field generator;
+ * GSN_ERR_ARG if shift is zero or shift^n = 1.  Device arrays, canonical. */
+int gsn_coset_quotient(int field, uint32_t* a, const uint32_t* b, const uint32_t* c, uint32_t log_n,
+                       const uint32_t* shift, void* stream);
+
+/* The whole H computation of the QAP witness map (libsnark's
+ * r1cs_to_qap_witness_map): a, b, c hold the evaluations of A, B, C on the
+ * domain <w> (natural order, default root); each is inverse-transformed,
+ * coset-transformed by `shift` (NULL: the field generator), combined by
+ * gsn_coset_quotient, and the result coset-inverse-transformed, leaving the
+ * n coefficients of H = (A B - C) / Z in `a`.  b and c are overwritten
+ * (coset evaluations).  Seven transforms and one pointwise kernel, queued on
+ * `stream`. */
+int gsn_qap_h(int field, uint32_t* a, uint32_t* b, uint32_t* c, uint32_t log_n, const uint32_t* shift,
+              void* stream);
+
 /* In-place element format conversion on device memory.
  *   GSN_TO_MONTGOMERY    x -> x*R mod p      (R = 2^(32*LIMBS))
  *   GSN_FROM_MONTGOMERY  x -> x*R^-1 mod p
@@ -266,6 +286,11 @@ int gsn_microbench_mont(int field, int schedule, int iters, double* muls_per_s);
  * threads per element; checks 256 products against the host arithmetic
  * first (GSN_ERR_STATE on a mismatch). */
 int gsn_microbench_mont_coop(int field, int lanes, int iters, double* muls_per_s);
+/* One-limb (p32) DIF butterflies per second on the whole GPU: variant 0 the
+ * compare-and-select forms, 1 the borrow-mask forms whose "+p" correction is
+ * a multiply-add.  Checks that both agree element by element and match the
+ * host arithmetic first (GSN_ERR_STATE on a mismatch). */
+int gsn_microbench_p32_butterfly(int variant, int iters, double* bfly_per_s);
 
 #ifdef __cplusplus
 }

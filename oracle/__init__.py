@@ -149,6 +149,33 @@ def coset_ntt(fid: int, data: np.ndarray, shift: int, omega: int | None = None, 
     return ntt(fid, array(fid, pre, like=data), omega, nthreads=nthreads)
 
 
+def coset_intt(fid: int, data: np.ndarray, shift: int, omega: int | None = None, *, nthreads: int = 0):
+    """Inverse of coset_ntt: inverse NTT, then x_i * shift^-i."""
+    p = MODULI[fid]
+    xs = ints(fid, intt(fid, data, omega, nthreads=nthreads))
+    sinv, s, out = pow(shift, p - 2, p), 1, []
+    for x in xs:
+        out.append((x * s) % p)
+        s = (s * sinv) % p
+    return array(fid, out, like=data)
+
+
+def qap_h(fid: int, a: np.ndarray, b: np.ndarray, c: np.ndarray, shift: int | None = None) -> np.ndarray:
+    """H = (A B - C) / (x^n - 1) of the QAP witness map, from the evaluations of A, B, C on the size-n
+    domain (the published algorithm of libsnark's r1cs_to_qap_witness_map, a third-party prover
+    that the reference's MNT4-753 types serve, cuda/device_field.h:443-447): interpolate A, B, C
+    (inverse NTT), evaluate them on the coset shift*<w> (coset NTT), divide A*B - C pointwise by
+    Z(shift w^i) = shift^n - 1, interpolate on the coset (coset inverse NTT)."""
+    p = MODULI[fid]
+    if shift is None:
+        shift = GENERATORS[fid]
+    n = np.asarray(a).size // LIMBS[fid]
+    ev = [ints(fid, coset_ntt(fid, intt(fid, x), shift)) for x in (a, b, c)]
+    zinv = pow((pow(shift, n, p) - 1) % p, p - 2, p)
+    h = [((x * y - z) * zinv) % p for x, y, z in zip(*ev)]
+    return coset_intt(fid, array(fid, h, like=a), shift)
+
+
 def arith(fid: int, op: str, a: int, b: int = 0, e: int = 0) -> int:
     code = {"mul": 0, "add": 1, "sub": 2, "pow": 3}[op]
     out = np.zeros(LIMBS[fid], dtype=np.uint32)

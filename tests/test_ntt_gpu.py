@@ -131,6 +131,51 @@ def test_host_path_best_fft(gsn, cuda_device):
         assert np.array_equal(a, x)
 
 
+def test_host_path_pinned(gsn, cuda_device):
+    """gsn_ntt_host on page-locked host memory (the buffer bench.py's e2e uses): forward, inverse and
+    coset forward match the oracle."""
+    import ctypes
+    cases = ((gsn.P32, 16), (gsn.BLS12_381, 8), (gsn.BLS12_381, 13), (gsn.MNT4_753, 4),
+             (gsn.MNT4_753, 12), (gsn.MNT4_753, 15))
+    for f, log_n in cases:
+        n = 1 << log_n
+        x = f.random_array(n, seed=SEED + 5 * log_n + f.fid)
+        buf = gsn.host_buffer(x.nbytes)
+        try:
+            arr = np.ctypeslib.as_array(ctypes.cast(buf, ctypes.POINTER(ctypes.c_uint32)),
+                                        shape=(x.size,)).reshape(x.shape)
+            arr[...] = x
+            gsn._lib.check(gsn.load().gsn_ntt_host(f.fid, buf.value, log_n, None, gsn.FORWARD, None))
+            assert np.array_equal(arr, O.ntt(f.fid, x).reshape(x.shape)), (f.name, log_n)
+            gsn._lib.check(gsn.load().gsn_ntt_host(f.fid, buf.value, log_n, None, gsn.INVERSE, None))
+            assert np.array_equal(arr, x), (f.name, log_n)
+            s = np.ascontiguousarray(f.to_limbs(f.generator), dtype=np.uint32)
+            gsn._lib.check(gsn.load().gsn_ntt_host(f.fid, buf.value, log_n, None, gsn.COSET_FORWARD,
+                                                   gsn._lib.u32p(s)))
+            assert np.array_equal(arr, O.coset_ntt(f.fid, x, f.generator).reshape(x.shape)), (f.name, log_n)
+        finally:
+            gsn.free_host_buffer(buf)
+
+
+@pytest.mark.parametrize("log_n", [12, 18, 22])
+def test_p32_four_byte_aligned_arrays(gsn, cuda_device, log_n):
+    """p32 data and scratch only 4-byte aligned (offset by one element) take the generic pass instead of
+    the 16-byte-vector kernel, and still match the oracle."""
+    import torch
+    f = gsn.P32
+    n = 1 << log_n
+    x = f.random_array(n, seed=SEED + log_n)
+    big = torch.zeros(n + 4, dtype=torch.int32, device="cuda")
+    d = big[1:n + 1]
+    d.copy_(torch.from_numpy(x.view(np.int32)))
+    scr = torch.zeros(n + 4, dtype=torch.int32, device="cuda")[1:n + 1]
+    assert d.data_ptr() % 16 == 4 and scr.data_ptr() % 16 == 4
+    gsn.ntt(f, d)
+    assert np.array_equal(gsn.to_host(d), O.ntt(0, x))
+    gsn.ntt(f, d, direction=gsn.INVERSE, scratch=scr)
+    assert np.array_equal(gsn.to_host(d), x)
+
+
 def test_deterministic_rerun(gsn, cuda_device):
     f = gsn.BLS12_381
     x = f.random_array(1 << 15, seed=SEED + 8)

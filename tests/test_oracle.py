@@ -90,6 +90,31 @@ def test_intt_roundtrip_and_coset(fid):
     assert O.ints(fid, O.coset_ntt(fid, x, g)) == want
 
 
+@pytest.mark.parametrize("fid", [0, 1, 2])
+def test_qap_h_is_exact_quotient(fid):
+    """For a satisfied system (c_i = a_i b_i on the domain) the oracle's H is the exact polynomial
+    quotient (A B - C) / (x^n - 1), checked with schoolbook products; its top coefficient is zero.
+    Also the coset inverse undoes the coset transform."""
+    rnd = random.Random(31 + fid)
+    p = O.MODULI[fid]
+    n = 32
+    a = [rnd.randrange(p) for _ in range(n)]
+    b = [rnd.randrange(p) for _ in range(n)]
+    c = [(x * y) % p for x, y in zip(a, b)]
+    H = O.ints(fid, O.qap_h(fid, O.array(fid, a), O.array(fid, b), O.array(fid, c)))
+    assert H[n - 1] == 0
+    A, B, C = (O.ints(fid, O.intt(fid, O.array(fid, v))) for v in (a, b, c))
+    lhs = O.schoolbook(fid, A, B)
+    for i, v in enumerate(C):
+        lhs[i] = (lhs[i] - v) % p
+    z = [p - 1] + [0] * (n - 1) + [1]  # x^n - 1
+    rhs = O.schoolbook(fid, H[: n - 1], z)
+    assert lhs[: len(rhs)] == rhs and all(v == 0 for v in lhs[len(rhs):])
+    x = O.array(fid, a)
+    s = rnd.randrange(2, p)
+    assert O.ints(fid, O.coset_intt(fid, O.coset_ntt(fid, x, s), s)) == a
+
+
 @pytest.mark.parametrize("fid", [0, 1])
 def test_ntt_polynomial_product(fid):
     rnd = random.Random(11 + fid)
