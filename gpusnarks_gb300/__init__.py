@@ -140,6 +140,17 @@ def qap_h(field, a, b, c, *, shift=None, stream=None):
     return a
 
 
+def fft_ref_compat(data, omega_limbs, log_cpus: int = 10, *, stream=None):
+    """The reference's host FFT dataflow (test/fft_host.h:56-118) over its own 24-limb Scalar arithmetic,
+    on the GPU, bit for bit (not a DFT).  ``data``: device tensor of n*24 raw limbs; ``omega_limbs``: 24
+    raw limbs."""
+    n = data.numel() // 24
+    w = np.ascontiguousarray(omega_limbs, dtype=np.uint32).reshape(-1)[:24].copy()
+    check(load().gsn_fft_ref_compat(data.data_ptr(), _log2_exact(n), u32p(w), int(log_cpus),
+                                    _stream_handle(stream)))
+    return data
+
+
 TO_MONTGOMERY, FROM_MONTGOMERY, REVERSE_LIMBS = 0, 1, 2
 
 

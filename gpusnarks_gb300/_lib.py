@@ -49,6 +49,7 @@ _SIGNATURES = [
                                           ctypes.c_uint32, _u32p, ctypes.c_void_p]),
     ("gsn_qap_h", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                  _u32p, ctypes.c_void_p]),
+    ("gsn_fft_ref_compat", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _u32p, ctypes.c_int, ctypes.c_void_p]),
     ("gsn_convert", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p]),
     ("gsn_synchronize", ctypes.c_int, [ctypes.c_void_p]),
     ("gsn_host_alloc", ctypes.c_int, [ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t]),

@@ -101,6 +101,63 @@ __global__ void mont_chain_kernel(uint32_t* sink, int iters) {
   sink[blockIdx.x * blockDim.x + threadIdx.x] = acc;
 }
 
+// out[i] = a[i] * b[i] * R^-1 with schedule S, for checking against the host arithmetic
+template <class P, int S>
+__global__ void mont_check_kernel(const uint32_t* a, const uint32_t* b, uint32_t* out, int count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= count) return;
+  Fe<P> x, y, r;
+#pragma unroll
+  for (int j = 0; j < P::N; ++j) {
+    x.l[j] = a[i * P::N + j];
+    y.l[j] = b[i * P::N + j];
+  }
+  fe_mul<P, S>(r, x, y);
+#pragma unroll
+  for (int j = 0; j < P::N; ++j) out[i * P::N + j] = r.l[j];
+}
+
+// 256 products of pseudo-random canonical operands (and the extremes 0, 1, p-1) against h_mont_mul
+template <class P, int S>
+static int check_mont(uint32_t* scratch_dev) {
+  constexpr int N = P::N, K = 256;
+  std::vector<uint32_t> a(K * N), b(K * N), got(K * N);
+  uint64_t st = 0x243F6A8885A308D3ull;
+  auto next = [&] {
+    st ^= st << 13;
+    st ^= st >> 7;
+    st ^= st << 17;
+    return (uint32_t)st;
+  };
+  for (int i = 0; i < K; ++i) {
+    for (int j = 0; j < N; ++j) {
+      a[i * N + j] = next();
+      b[i * N + j] = next();
+    }
+    a[i * N + N - 1] &= 0xFFFFu;  // below every modulus here
+    b[i * N + N - 1] &= 0xFFFFu;
+  }
+  for (int j = 0; j < N; ++j) {  // extremes: 0 * x, 1 * x, (p-1) * (p-1)
+    a[j] = 0u;
+    a[N + j] = j == 0 ? 1u : 0u;
+    a[2 * N + j] = b[2 * N + j] = P::mod(j) - (j == 0 ? 1u : 0u);
+  }
+  uint32_t* da = scratch_dev;
+  uint32_t* db = da + K * N;
+  uint32_t* dout = db + K * N;
+  GSN_CUDA(cudaMemcpy(da, a.data(), a.size() * 4, cudaMemcpyHostToDevice));
+  GSN_CUDA(cudaMemcpy(db, b.data(), b.size() * 4, cudaMemcpyHostToDevice));
+  mont_check_kernel<P, S><<<(K + 127) / 128, 128>>>(da, db, dout, K);
+  GSN_CUDA(cudaMemcpy(got.data(), dout, got.size() * 4, cudaMemcpyDeviceToHost));
+  count_launches(1);
+  for (int i = 0; i < K; ++i) {
+    const HFe<P> want = h_mont_mul<P>(h_from_limbs<P>(&a[i * N]), h_from_limbs<P>(&b[i * N]));
+    if (std::memcmp(want.l, &got[i * N], N * 4) != 0)
+      return set_error(GSN_ERR_STATE, "Montgomery schedule %d disagrees with the host at product %d", S, i);
+  }
+  return GSN_OK;
+}
+
 template <class P, int S>
 static int run_mont_bench(int iters, double* muls_per_s) {
   int dev = 0, sms = 0, per_sm = 0;
@@ -110,8 +167,13 @@ static int run_mont_bench(int iters, double* muls_per_s) {
   GSN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mont_chain_kernel<P, S>, block, 0));
   const int grid = sms * std::max(per_sm, 1);
   uint32_t* sink = nullptr;
-  int rc = dev_alloc((void**)&sink, (size_t)grid * block * sizeof(uint32_t));
+  int rc = dev_alloc((void**)&sink, std::max((size_t)grid * block, (size_t)3 * 256 * P::N) * sizeof(uint32_t));
   if (rc) return rc;
+  rc = check_mont<P, S>(sink);
+  if (rc) {
+    dev_free(sink);
+    return rc;
+  }
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -478,13 +540,15 @@ extern "C" int gsn_microbench_mont_coop(int field, int lanes, int iters, double*
 }
 
 extern "C" int gsn_microbench_mont(int field, int schedule, int iters, double* muls_per_s) {
-  if (iters <= 0 || !muls_per_s || (schedule != 0 && schedule != 1))
+  if (iters <= 0 || !muls_per_s || schedule < 0 || schedule > 2)
     return set_error(GSN_ERR_ARG, "bad microbenchmark arguments");
-  switch (field * 2 + schedule) {
-    case GSN_BLS12_381_FR * 2 + 0: return run_mont_bench<FieldBLS12_381, 0>(iters, muls_per_s);
-    case GSN_BLS12_381_FR * 2 + 1: return run_mont_bench<FieldBLS12_381, 1>(iters, muls_per_s);
-    case GSN_MNT4753_FR * 2 + 0: return run_mont_bench<FieldMNT4_753, 0>(iters, muls_per_s);
-    case GSN_MNT4753_FR * 2 + 1: return run_mont_bench<FieldMNT4_753, 1>(iters, muls_per_s);
+  switch (field * 3 + schedule) {
+    case GSN_BLS12_381_FR * 3 + 0: return run_mont_bench<FieldBLS12_381, 0>(iters, muls_per_s);
+    case GSN_BLS12_381_FR * 3 + 1: return run_mont_bench<FieldBLS12_381, 1>(iters, muls_per_s);
+    case GSN_BLS12_381_FR * 3 + 2: return run_mont_bench<FieldBLS12_381, 2>(iters, muls_per_s);
+    case GSN_MNT4753_FR * 3 + 0: return run_mont_bench<FieldMNT4_753, 0>(iters, muls_per_s);
+    case GSN_MNT4753_FR * 3 + 1: return run_mont_bench<FieldMNT4_753, 1>(iters, muls_per_s);
+    case GSN_MNT4753_FR * 3 + 2: return run_mont_bench<FieldMNT4_753, 2>(iters, muls_per_s);
     default: return set_error(GSN_ERR_FIELD, "Montgomery microbenchmark covers the multi-limb fields");
   }
 }

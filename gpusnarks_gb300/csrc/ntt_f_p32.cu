@@ -8,8 +8,9 @@ namespace gsn {
 const FieldOps kOpsP32 = make_field_ops<FieldP32>(28, 16);
 
 cudaError_t launch_p32_pass(const P32Args& A, int e_log, int block, int grid_cap, cudaStream_t s) {
-  if (e_log == 3) return p32_launch_et<3>(A, block, grid_cap, s);
-  if (e_log == 4) return p32_launch_et<4>(A, block, grid_cap, s);
+  const bool narrow = A.log_j == 2;  // 4 columns per tile; 8 and 16 are in the c1 units
+  if (e_log == 3) return narrow ? p32_launch_et_cg<3, 0>(A, block, grid_cap, s) : p32_launch_et_cg<3, 1>(A, block, grid_cap, s);
+  if (e_log == 4) return narrow ? p32_launch_et_cg<4, 0>(A, block, grid_cap, s) : p32_launch_et_cg<4, 1>(A, block, grid_cap, s);
   return cudaErrorInvalidValue;
 }
 }  // namespace gsn

@@ -508,12 +508,13 @@ __global__ void __launch_bounds__(512) ntt_p32_fixed_kernel(P32Args A) {
   }
 }
 
-// Launchers.  The kernels for one sub-step size ET are instantiated in one
-// translation unit each (ntt_p32_e3.cu, ntt_p32_e4.cu) so they compile in
-// parallel: fixed-radix kernels for radix 2^8..2^13 with 4 or 8 columns per
-// tile, the runtime-radix kernel for everything else.
-template <int ET>
-cudaError_t p32_launch_et(const P32Args& A, int block, int grid_cap, cudaStream_t s);
+// Launchers.  The kernels for one sub-step size ET and one column-group width
+// 2^LCG are instantiated in one translation unit each (ntt_p32_e{3,4}_c{0,1}.cu)
+// so they compile in parallel: fixed-radix kernels (plain and column prefetch)
+// for radix 2^8..2^13, the runtime-radix kernel for everything else (and for
+// 16-column tiles, in the c1 units).
+template <int ET, int LCG>
+cudaError_t p32_launch_et_cg(const P32Args& A, int block, int grid_cap, cudaStream_t s);
 
 #ifdef GSN_P32_INSTANTIATE_ET
 namespace p32 {
@@ -521,12 +522,13 @@ namespace p32 {
 // the CTA's next tile), keeping at least two CTAs' worth of shared memory per SM.
 constexpr size_t kPipeTileMax = 48 * 1024;
 
+// buffers: tile-sized shared-memory buffers the kernel uses (1 plain, 2 with the column prefetch)
 template <class K>
-cudaError_t launch_kernel(K k, const P32Args& A, int block, int grid_cap, cudaStream_t s, bool pipe = false) {
+cudaError_t launch_kernel(K k, const P32Args& A, int block, int grid_cap, cudaStream_t s, int buffers = 1) {
   P32Args B = A;
-  B.pipe = pipe ? 1 : 0;
+  B.pipe = buffers > 1 ? 1 : 0;
   const size_t tile = ((size_t)1 << (A.log_r + A.log_j)) * sizeof(uint32_t);
-  const size_t smem = pipe ? 2 * tile : tile;
+  const size_t smem = buffers * tile;
   if (smem > kDefaultSmemOptIn) {
     cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
@@ -548,7 +550,7 @@ cudaError_t launch_fixed(const P32Args& A, int block, int grid_cap, cudaStream_t
     if (A.log_r == RL) {
       const size_t tile = ((size_t)1 << (A.log_r + A.log_j)) * sizeof(uint32_t);
       if (!A.last && tile <= kPipeTileMax && pipe_enabled())
-        return launch_kernel(ntt_p32_pipe_kernel<RL, ET, LCG>, A, block, grid_cap, s, true);
+        return launch_kernel(ntt_p32_pipe_kernel<RL, ET, LCG>, A, block, grid_cap, s, 2);
       return launch_kernel(ntt_p32_fixed_kernel<RL, ET, LCG>, A, block, grid_cap, s);
     }
     return launch_fixed<ET, LCG, RL + 1>(A, block, grid_cap, s);
@@ -559,14 +561,15 @@ cudaError_t launch_fixed(const P32Args& A, int block, int grid_cap, cudaStream_t
 }  // namespace p32
 
 template <>
-cudaError_t p32_launch_et<GSN_P32_INSTANTIATE_ET>(const P32Args& A, int block, int grid_cap, cudaStream_t s) {
+cudaError_t p32_launch_et_cg<GSN_P32_INSTANTIATE_ET, GSN_P32_INSTANTIATE_LCG>(const P32Args& A, int block,
+                                                                            int grid_cap, cudaStream_t s) {
   constexpr int ET = GSN_P32_INSTANTIATE_ET;
-  switch (A.log_j - 2) {
-    case 0: return p32::launch_fixed<ET, 0, 8>(A, block, grid_cap, s);
-    case 1: return p32::launch_fixed<ET, 1, 8>(A, block, grid_cap, s);
-    case 2: return p32::launch_kernel(ntt_p32_kernel<ET, 2>, A, block, grid_cap, s);
-    default: return cudaErrorInvalidValue;
+  constexpr int LCG = GSN_P32_INSTANTIATE_LCG;
+  if (A.log_j - 2 == LCG) return p32::launch_fixed<ET, LCG, 8>(A, block, grid_cap, s);
+  if constexpr (LCG == 1) {
+    if (A.log_j - 2 == 2) return p32::launch_kernel(ntt_p32_kernel<ET, 2>, A, block, grid_cap, s);
   }
+  return cudaErrorInvalidValue;
 }
 #endif
 

@@ -134,6 +134,18 @@ int gsn_coset_quotient(int field, uint32_t* a, const uint32_t* b, const uint32_t
 int gsn_qap_h(int field, uint32_t* a, uint32_t* b, uint32_t* c, uint32_t log_n, const uint32_t* shift,
               void* stream);
 
+/* Reference-compatible transform: the reference's host FFT
+ * _basic_parallel_radix2_FFT_inner(a, omega, log_cpus) (test/fft_host.h:56-118)
+ * run on the GPU with the reference's own fields::Scalar arithmetic and
+ * butterfly, so the output equals, bit for bit, what the reference computes
+ * (test/main.cpp:71 calls it with log_cpus = 10).  That output is not a DFT:
+ * the Scalar product is not a modular product (m_inv, 24-byte normalisation)
+ * and the butterfly uses the twiddle in place of w * hi.  data: n = 2^log_n
+ * raw 24-limb Scalar values (im_rep) on the device, 16-byte aligned,
+ * log_n <= 24; omega: 24 raw limbs; log_cpus in [0, 16].  Asynchronous on
+ * `stream`.  Use gsn_ntt for the transform itself. */
+int gsn_fft_ref_compat(uint32_t* data, uint32_t log_n, const uint32_t* omega, int log_cpus, void* stream);
+
 /* In-place element format conversion on device memory.
  *   GSN_TO_MONTGOMERY    x -> x*R mod p      (R = 2^(32*LIMBS))
  *   GSN_FROM_MONTGOMERY  x -> x*R^-1 mod p
@@ -280,7 +292,9 @@ uint64_t gsn_kernel_launch_count(void);
  * multiply-adds per second, per SM per clock, and the SM clock seen. */
 int gsn_microbench_imad(int iters, double* mads_per_s, double* mads_per_clk_sm, double* sm_mhz);
 /* Throughput (products per second, all SMs) of the multi-limb Montgomery
- * product with schedule 0 (row chains) or 1 (even/odd accumulators). */
+ * product with schedule 0 (row chains), 1 (even/odd accumulators merged every
+ * row) or 2 (split accumulators, carried merge); first checks 256 products of
+ * that schedule against the host arithmetic (GSN_ERR_STATE on a mismatch). */
 int gsn_microbench_mont(int field, int schedule, int iters, double* muls_per_s);
 /* Same for the cooperative MNT4-753 product split over `lanes` (2 or 4)
  * threads per element; checks 256 products against the host arithmetic
