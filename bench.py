@@ -48,6 +48,10 @@ HEADLINE_LOG_N = 18
 SEED = 0x5EED0000
 PEAKS = ROOT / "MEASURED_PEAKS.json"
 PUBLISHED_REF_768_2_18_S = 21.42  # README.md:46, GTX 1060, the reference's own (non-DFT) dataflow
+# MNT4-753 q, the modulus the reference's fields::Scalar compiles in (cuda/device_field.h:62-65)
+REF_Q = int("41898490967918953402344214791240637128170709919953949071783502921025352812571106773058"
+            "893763790338921418070971888253786114353726529584385201591605722013126468931404347949"
+            "840543007986327743462853720628051692141265303114721689601")
 
 
 # --------------------------------------------------------------------------- utils
@@ -148,12 +152,13 @@ def imad_peak(g) -> dict:
 
 def montgomery_schedules(g, iters: int = 2000) -> dict:
     """Montgomery products per second on the whole GPU for the one-thread schedules (0 row chains,
-    1 even/odd accumulators) and the 24-limb product split over 2 or 4 cooperating lanes."""
+    1 even/odd accumulators merged every row, 2 split accumulators with a carried merge) and the
+    24-limb product split over 2 or 4 cooperating lanes."""
     lib = g.load()
     out = {}
     for name, fid in (("bls12_381_fr", 1), ("mnt4753_fr", 2)):
         per = {}
-        for sched in (0, 1):
+        for sched in (0, 1, 2):
             v = ctypes.c_double()
             g._lib.check(lib.gsn_microbench_mont(fid, sched, iters, ctypes.byref(v)))
             per[f"thread_schedule{sched}_G_per_s"] = round(v.value / 1e9, 3)
@@ -163,6 +168,28 @@ def montgomery_schedules(g, iters: int = 2000) -> dict:
                 g._lib.check(lib.gsn_microbench_mont_coop(fid, lanes, iters, ctypes.byref(v)))
                 per[f"coop_{lanes}_lanes_G_per_s"] = round(v.value / 1e9, 3)
         out[name] = per
+    return out
+
+
+def ref_compat_shipped_call(g, torch) -> dict:
+    """The reference's shipped call (test/main.cpp:45-71: every input Scalar(1234), omega = the raw limbs
+    of its modulus, log_cpus = 10) through gsn_fft_ref_compat on the GPU at n = 2^12 and 2^16.  The
+    CPU restatement of the same dataflow is timed in cpu_baseline()."""
+    q = np.array([(REF_Q >> (32 * i)) & 0xFFFFFFFF for i in range(24)], dtype=np.uint32)
+    out = {"log_cpus": 10}
+    for log_n in (12, 16):
+        data = np.zeros((1 << log_n, 24), dtype=np.uint32)
+        data[:, 0] = 1234
+        d = g.to_device(data)
+        g.fft_ref_compat(d, q, 10)  # warm
+        torch.cuda.synchronize()
+        d.copy_(g.to_device(data))
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        g.fft_ref_compat(d, q, 10)
+        e.record()
+        e.synchronize()
+        out[f"gpu_ms_2^{log_n}"] = round(s.elapsed_time(e), 3)
     return out
 
 
@@ -370,6 +397,10 @@ def run_gpu(args, rank, local, ws):
             extra["serving"] = {"error": str(exc)}
         extra["imad_microbench"] = ip
         extra["montgomery_schedules"] = montgomery_schedules(g)
+        try:
+            extra["ref_compat_shipped_call"] = ref_compat_shipped_call(g, torch)
+        except Exception as exc:  # report, do not hide
+            extra["ref_compat_shipped_call"] = {"error": str(exc)}
         line["extra"] = extra
     return line
 
@@ -394,10 +425,20 @@ def cpu_baseline(args) -> dict:
         ts.append(time.perf_counter() - t0)
         reps += 1
     t = float(np.median(ts))
+    # the reference's shipped call (test/main.cpp:45-71) over its own Scalar arithmetic, at n = 2^12
+    shipped = np.zeros((1 << 12, 24), dtype=np.uint32)
+    shipped[:, 0] = 1234
+    t0 = time.perf_counter()
+    oracle.refscalar_fft(shipped, oracle.to_limbs(3, REF_Q), 10, nthreads=threads)
+    shipped_ms = (time.perf_counter() - t0) * 1e3
     return {"value": round(n / t / 1e6, 5), "unit": "Melem/s", "cores": threads, "kind": "port",
             "sample": f"full n=2^18 MNT4-753 r transform x{reps} (median), num_cpus decomposition "
                       f"log_cpus={log_cpus}, {threads} OpenMP threads; oracle/oracle.cpp restating "
-                      "test/fft_host.h with the fixed butterfly"}
+                      "test/fft_host.h with the fixed butterfly",
+            "shipped_call_2^12_ms": round(shipped_ms, 1),
+            "shipped_call": "test/main.cpp:45-71 at n=2^12 (inputs Scalar(1234), omega = Scalar(_mod), "
+                            "log_cpus=10) over the restated reference Scalar, all threads; "
+                            "extra.ref_compat_shipped_call times the same on the GPU"}
 
 
 def run_reference(args, rank, ws):
