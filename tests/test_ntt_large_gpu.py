@@ -126,3 +126,37 @@ def _oracle_intt_p32(X: np.ndarray) -> np.ndarray:
     y = O.fft(0, X, pow(w, P - 2, P), log_cpus=3)
     ninv = pow(n, P - 2, P)
     return ((y.astype(np.uint64) * np.uint64(ninv)) % np.uint64(P)).astype(np.uint32)
+
+
+def _limb_sum(arr: np.ndarray, sign: np.ndarray | None = None) -> int:
+    """sum_j s_j x_j as an integer, x given as (n, L) little-endian uint32 limbs, s_j in {+1, -1}: column
+    sums in uint64 (each < 2^32 * n <= 2^58), combined as a big integer."""
+    a = arr.astype(np.uint64)
+    if sign is None:
+        cols = a.sum(axis=0, dtype=np.uint64)
+        return sum(int(c) << (32 * i) for i, c in enumerate(cols))
+    pos = a[sign > 0].sum(axis=0, dtype=np.uint64)
+    neg = a[sign < 0].sum(axis=0, dtype=np.uint64)
+    return sum((int(c) - int(d)) << (32 * i) for i, (c, d) in enumerate(zip(pos, neg)))
+
+
+@pytest.mark.parametrize("fname,log_n", [("bls12_381_fr", 26), ("mnt4753_fr", 24), ("bls12_381_fr", 23)])
+def test_big_field_max_size_properties(gsn, cuda_device, fname, log_n):
+    """The largest transforms of the multi-limb fields (2^26 x 32 B = 2 GiB, 2^24 x 96 B = 1.5 GiB):
+    X[0] = sum x and X[n/2] = sum (-1)^j x_j (w^(n/2) = -1), both from exact limb-column sums, and the
+    inverse round trip, bit for bit on the device."""
+    import torch
+    from gpusnarks_gb300.batch import fill_random
+    f = gsn.FIELDS[fname]
+    n = 1 << log_n
+    d = torch.empty(n * f.limbs, dtype=torch.int32, device="cuda")
+    fill_random(f, d, 0x5EED0000 + log_n)
+    x0 = d.clone()
+    x = gsn.to_host(d).reshape(n, f.limbs)
+    gsn.ntt(f, d)
+    X = gsn.to_host(d).reshape(n, f.limbs)
+    assert f.from_limbs(X[0]) == _limb_sum(x) % f.p
+    sign = np.where(np.arange(n) % 2 == 0, 1, -1)
+    assert f.from_limbs(X[n // 2]) == _limb_sum(x, sign) % f.p
+    gsn.ntt(f, d, direction=gsn.INVERSE)
+    assert torch.equal(d, x0)
