@@ -109,7 +109,8 @@ struct Req {
   int rc = GSN_OK;
   std::string err;  // message of a failure, captured on the scheduler thread
   cudaEvent_t ev = nullptr;
-  Clock::time_point t_submit, t_done;
+  // phase times: submitted, admitted (memory granted, upload queued), uploaded, launched, computed, done
+  Clock::time_point t_submit, t_admit, t_ready, t_launch, t_computed, t_done;
 };
 
 struct Slot {
@@ -212,6 +213,7 @@ bool try_admit(gsn_server* S, Req& q) {
     return true;
   }
   q.st = kCopyIn;
+  q.t_admit = Clock::now();
   return true;
 }
 
@@ -296,7 +298,11 @@ void launch(gsn_server* S, int si) {
   }
   count_launches(1);
   ++S->launches;
-  for (uint64_t id : ids) S->reqs[id].st = kRunning;
+  const Clock::time_point t_launch = Clock::now();
+  for (uint64_t id : ids) {
+    S->reqs[id].st = kRunning;
+    S->reqs[id].t_launch = t_launch;
+  }
   sl.reqs = ids;
   sl.busy = true;
   if (S->inflight++ == 0) S->busy_since = Clock::now();
@@ -305,8 +311,10 @@ void launch(gsn_server* S, int si) {
 
 void retire(gsn_server* S, Slot& sl) {
   const uint32_t st = *sl.status_host;
+  const Clock::time_point t_computed = Clock::now();
   for (uint64_t id : sl.reqs) {
     Req& q = S->reqs[id];
+    q.t_computed = t_computed;
     free_mem(S, q, false);
     if (st) {
       finish(S, q, kFailed, set_error((int)st, "a bounded device wait in the batch kernel gave up"));
@@ -358,6 +366,7 @@ void scheduler(gsn_server* S) {
     for (auto it = S->copyin.begin(); it != S->copyin.end();) {
       if (cudaEventQuery(S->reqs[*it].ev) == cudaSuccess) {
         S->reqs[*it].st = kReady;
+        S->reqs[*it].t_ready = Clock::now();
         S->ready.push_back(*it);
         it = S->copyin.erase(it);
         progressed = true;
@@ -578,6 +587,11 @@ int gsn_server_destroy(gsn_server* S) {
 
 int gsn_server_run_trace(gsn_server* S, const gsn_trace_entry* trace, size_t n, double* latencies_out,
                          double* makespan_s) {
+  return gsn_server_run_trace_phases(S, trace, n, latencies_out, nullptr, makespan_s);
+}
+
+int gsn_server_run_trace_phases(gsn_server* S, const gsn_trace_entry* trace, size_t n, double* latencies_out,
+                                double* phases_out, double* makespan_s) {
   if (!S || (!trace && n)) return set_error(GSN_ERR_ARG, "null argument");
   std::vector<uint64_t> ids(n, 0);
   std::vector<int> rcs(n, GSN_OK);
@@ -612,6 +626,18 @@ int gsn_server_run_trace(gsn_server* S, const gsn_trace_entry* trace, size_t n, 
     const Clock::time_point arr = t0 + std::chrono::duration_cast<Clock::duration>(
                                            std::chrono::duration<double>(trace[i].arrival_s));
     if (latencies_out) latencies_out[i] = rc ? -1.0 : seconds(q.t_done - arr);
+    if (phases_out) {
+      double* ph = phases_out + 5 * i;
+      if (rc) {
+        for (int k = 0; k < 5; ++k) ph[k] = -1.0;
+      } else {
+        ph[0] = seconds(q.t_admit - arr);
+        ph[1] = seconds(q.t_ready - q.t_admit);
+        ph[2] = seconds(q.t_launch - q.t_ready);
+        ph[3] = seconds(q.t_computed - q.t_launch);
+        ph[4] = seconds(q.t_done - q.t_computed);
+      }
+    }
     if (q.t_done > last) last = q.t_done;
   }
   if (makespan_s) *makespan_s = seconds(last - t0);

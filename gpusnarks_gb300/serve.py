@@ -43,7 +43,12 @@ _SIGS = [
     ("gsn_server_destroy", [ctypes.c_void_p]),
     ("gsn_server_run_trace", [ctypes.c_void_p, ctypes.POINTER(TraceEntry), ctypes.c_size_t,
                               ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    ("gsn_server_run_trace_phases", [ctypes.c_void_p, ctypes.POINTER(TraceEntry), ctypes.c_size_t,
+                                     ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double),
+                                     ctypes.POINTER(ctypes.c_double)]),
 ]
+
+PHASES = ("queue", "upload", "wait_launch", "compute", "download")
 
 
 def _lib():
@@ -98,12 +103,19 @@ class Server:
         check(self.lib.gsn_server_get_stats(self.h, ctypes.byref(st)))
         return {k: getattr(st, k) for k, _ in ServerStats._fields_}
 
-    def run_trace(self, entries) -> tuple[np.ndarray, float]:
+    def run_trace(self, entries, phases: bool = False):
+        """Replay (arrival, Request) entries.  Returns (latencies, makespan), and with phases=True also an
+        (n, 5) array of seconds per request spent in PHASES."""
         arr = (TraceEntry * len(entries))(*entries)
         lat = (ctypes.c_double * len(entries))()
         mk = ctypes.c_double()
-        check(self.lib.gsn_server_run_trace(self.h, arr, len(entries), lat, ctypes.byref(mk)))
-        return np.array(lat[:], dtype=np.float64), mk.value
+        if not phases:
+            check(self.lib.gsn_server_run_trace(self.h, arr, len(entries), lat, ctypes.byref(mk)))
+            return np.array(lat[:], dtype=np.float64), mk.value
+        ph = (ctypes.c_double * (5 * len(entries)))()
+        check(self.lib.gsn_server_run_trace_phases(self.h, arr, len(entries), lat, ph, ctypes.byref(mk)))
+        return (np.array(lat[:], dtype=np.float64), mk.value,
+                np.array(ph[:], dtype=np.float64).reshape(len(entries), 5))
 
     def close(self) -> None:
         if self.h:
@@ -155,7 +167,7 @@ def bench_serving(g, torch, *, seconds: float = 1.0, rate: float = 2000.0, budge
         for (t, fid, k, d) in trace:
             pin, pout = bufs[(fid, k)]
             entries.append(TraceEntry(t, Request(fid, k, d, None, pin.value, pout.value)))
-        lat, makespan = srv.run_trace(entries)
+        lat, makespan, ph = srv.run_trace(entries, phases=True)
         st = srv.stats()
     finally:
         srv.close()
@@ -170,4 +182,8 @@ def bench_serving(g, torch, *, seconds: float = 1.0, rate: float = 2000.0, budge
             "throughput_req_s": round(len(trace) / makespan, 1),
             "throughput_Melem_s": round(elements / makespan / 1e6, 2),
             "launches": st["launches"], "device_bytes_peak": st["device_bytes_peak"],
+            "phase_ms_p50": {k: round(float(np.percentile(ph[:, i], 50)) * 1e3, 3) for i, k in enumerate(PHASES)},
+            "phase_ms_p99": {k: round(float(np.percentile(ph[:, i], 99)) * 1e3, 3) for i, k in enumerate(PHASES)},
+            "p99_request_phases_ms": {k: round(float(ph[int(np.argsort(lat)[int(0.99 * (len(lat) - 1))]), i]) * 1e3, 3)
+                                      for i, k in enumerate(PHASES)},
             "budget_bytes": int(budget_gb * (1 << 30)), "max_inflight": max_inflight}

@@ -271,6 +271,14 @@ typedef struct gsn_trace_entry {
  * *makespan_s = first arrival to last completion. */
 int gsn_server_run_trace(gsn_server* s, const gsn_trace_entry* trace, size_t n, double* latencies_out,
                          double* makespan_s);
+/* Same, and (phases_out nullable, n x 5 doubles) where each request's time
+ * went, in seconds: [0] scheduled arrival to admission (memory granted,
+ * upload queued), [1] upload, [2] uploaded to launched (waiting for a launch
+ * slot), [3] launched to launch finished (GPU compute, shared with the other
+ * requests packed into the same launch), [4] launch finished to done (result
+ * download).  A failed request gets -1 in every phase. */
+int gsn_server_run_trace_phases(gsn_server* s, const gsn_trace_entry* trace, size_t n, double* latencies_out,
+                                double* phases_out, double* makespan_s);
 
 /* Fill device memory with uniform elements of [0, p): element i, limb j are
  * drawn from splitmix64 of (seed, i, attempt) with rejection sampling;

@@ -92,9 +92,13 @@ def test_run_trace_small(gsn, cuda_device):
     try:
         srv.warmup(1, 6, 11)
         srv.warmup(2, 6, 11)
-        lat, makespan = srv.run_trace(entries)
+        lat, makespan, ph = srv.run_trace(entries, phases=True)
     finally:
         srv.close()
     assert (lat > 0).all() and makespan > 0
     for o, w in zip(outs, want):
         assert np.array_equal(o, w)
+    # phase times: each non-negative, and together the request's latency (clock reads differ by ~us)
+    assert ph.shape == (len(entries), 5)
+    assert (ph[:, 1:] >= 0).all() and (ph[:, 0] > -1e-3).all()
+    assert np.allclose(ph.sum(axis=1), lat, atol=1e-4)
