@@ -89,6 +89,21 @@ __device__ __forceinline__ uint32_t mul1(uint32_t a, uint32_t b) {
   uint32_t r = hi - mh;
   return (hi < mh) ? r + p : r;
 }
+// mul1 with w' = w * p^-1 mod 2^32 supplied: Montgomery's m = (a w mod 2^32) p^-1 equals a w' mod 2^32,
+// so a product with a reused w costs one multiply less.  Same result as mul1(a, w).
+template <class P>
+__device__ __forceinline__ uint32_t mul1_pre(uint32_t a, uint32_t w, uint32_t wp) {
+  constexpr uint32_t p = P::mod(0);
+  const uint32_t hi = ptx::mul_hi(a, w);
+  const uint32_t m = a * wp;
+  const uint32_t mh = ptx::mul_hi(m, p);
+  const uint32_t r = hi - mh;
+  return (hi < mh) ? r + p : r;
+}
+template <class P>
+__device__ __forceinline__ uint32_t mul1_wp(uint32_t w) {  // w' for mul1_pre
+  return w * (0u - P::PINV);
+}
 template <class P>
 __device__ __forceinline__ uint32_t add1(uint32_t a, uint32_t b) {
   constexpr uint32_t p = P::mod(0);

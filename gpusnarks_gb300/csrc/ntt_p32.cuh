@@ -75,6 +75,15 @@ __device__ __forceinline__ uint4 mul4(uint4 a, uint32_t w) {
 __device__ __forceinline__ uint4 mul4v(uint4 a, uint4 w) {
   return make_uint4(mm(a.x, w.x), mm(a.y, w.y), mm(a.z, w.z), mm(a.w, w.w));
 }
+// the same with w' = w p^-1 precomputed for a reused w (mul1_pre)
+__device__ __forceinline__ uint4 mul4_pre(uint4 a, uint32_t w, uint32_t wp) {
+  return make_uint4(mul1_pre<F>(a.x, w, wp), mul1_pre<F>(a.y, w, wp), mul1_pre<F>(a.z, w, wp),
+                    mul1_pre<F>(a.w, w, wp));
+}
+__device__ __forceinline__ uint4 mul4v_pre(uint4 a, uint4 w, uint4 wp) {
+  return make_uint4(mul1_pre<F>(a.x, w.x, wp.x), mul1_pre<F>(a.y, w.y, wp.y), mul1_pre<F>(a.z, w.z, wp.z),
+                    mul1_pre<F>(a.w, w.w, wp.w));
+}
 
 // DIF butterfly of the last stage, whose twiddle is w^0 = 1: (a, b) -> (a + b, a - b)
 __device__ __forceinline__ void bfly4_unit(uint4& a, uint4& b) {
@@ -91,8 +100,8 @@ __device__ __forceinline__ void bfly4_unit(uint4& a, uint4& b) {
   b = d;
 }
 
-// DIF butterfly on 4 columns: (a, b) -> (a + b, (a - b) * w)
-__device__ __forceinline__ void bfly4(uint4& a, uint4& b, uint32_t w) {
+// DIF butterfly on 4 columns: (a, b) -> (a + b, (a - b) * w), wp = w p^-1 (mul1_wp)
+__device__ __forceinline__ void bfly4(uint4& a, uint4& b, uint32_t w, uint32_t wp) {
   uint4 s, d;
   s.x = add1<F>(a.x, b.x);
   d.x = sub1<F>(a.x, b.x);
@@ -103,7 +112,7 @@ __device__ __forceinline__ void bfly4(uint4& a, uint4& b, uint32_t w) {
   s.w = add1<F>(a.w, b.w);
   d.w = sub1<F>(a.w, b.w);
   a = s;
-  b = mul4(d, w);
+  b = mul4_pre(d, w, wp);
 }
 
 __device__ __forceinline__ uint32_t tw_n(const P32Args& A, uint64_t e) {
@@ -131,10 +140,11 @@ __device__ __forceinline__ void substep(uint4* sm, const uint32_t* __restrict__ 
 #pragma unroll
     for (int t = 0; t < (E >> (q + 1)); ++t) {
       const uint32_t w = __ldg(twt + ((((uint32_t)t << ls) + low) << (s0 + q)));
+      const uint32_t wp = mul1_wp<F>(w);
 #pragma unroll
       for (int g = 0; g < (1 << q); ++g) {
         const int m = g * (E >> q) + t;
-        bfly4(x[m], x[m + (E >> (q + 1))], w);
+        bfly4(x[m], x[m + (E >> (q + 1))], w, wp);
       }
     }
   }
@@ -305,10 +315,11 @@ __device__ __forceinline__ void substep_fixed(uint4* sm, const uint32_t* __restr
 #pragma unroll
     for (int t = 0; t < (E >> (q + 1)); ++t) {
       const uint32_t w = __ldg(tq + ((uint32_t)t << (LS + S0 + q)));
+      const uint32_t wp = mul1_wp<F>(w);
 #pragma unroll
       for (int g = 0; g < (1 << q); ++g) {
         const int m = g * (E >> q) + t;
-        bfly4(x[m], x[m + (E >> (q + 1))], w);
+        bfly4(x[m], x[m + (E >> (q + 1))], w, wp);
       }
     }
   }
@@ -378,11 +389,12 @@ __device__ __forceinline__ void store_fourstep(const P32Args& A, const uint4* sm
   uint4 w = make_uint4(tw_n(A, e0 * k0), tw_n(A, e1 * k0), tw_n(A, e2 * k0), tw_n(A, e3 * k0));
   uint4 st = make_uint4(0u, 0u, 0u, 0u);
   if (k0 + dk < R) st = make_uint4(tw_n(A, e0 * dk), tw_n(A, e1 * dk), tw_n(A, e2 * dk), tw_n(A, e3 * dk));
+  const uint4 stp = make_uint4(mul1_wp<F>(st.x), mul1_wp<F>(st.y), mul1_wp<F>(st.z), mul1_wp<F>(st.w));
   for (uint32_t k = k0; k < R; k += dk) {
     uint4 x = sm[chunk_of<LCG>(brev(k, RL), cg)];
     x = mul4v(x, w);
     *reinterpret_cast<uint4*>(A.dst + base + ((uint64_t)k << A.log_inner) + 4 * cg) = x;
-    if (k + dk < R) w = mul4v(w, st);
+    if (k + dk < R) w = mul4v_pre(w, st, stp);
   }
 }
 

@@ -4,17 +4,20 @@
 // One scheduler thread owns all device work.  Each iteration it
 //   1. admits pending requests in arrival order while their polynomial and
 //      scratch fit in the device arena (the HBM budget), starting their
-//      host->device copies on the copy-in stream (a request that does not fit
-//      lets up to kBackfill later, smaller ones go first);
+//      host->device copies (a request that does not fit lets up to kBackfill
+//      later, smaller ones go first);
 //   2. marks copied-in requests ready;
 //   3. retires finished launches: scratch returns to the arena, results are
-//      copied out on the copy-out stream (or stay resident for a later fetch);
-//   4. while a launch slot is free, packs every ready request of one field
-//      (oldest first, up to max_batch_jobs) into one persistent launch on that
-//      slot's stream.
-// Up to max_inflight launches run at once, so requests that arrive while
-// others are on the GPU start as soon as memory and a slot free up.  Twiddle
-// tables come from the process-wide cache and stay resident.
+//      copied out (or stay resident for a later fetch);
+//   4. while a launch slot is free, packs ready requests of one field (oldest
+//      first, up to max_batch_jobs and max_launch_work) into one persistent
+//      launch on that slot's stream; a lone request whose work exceeds
+//      max_launch_work runs as per-pass launches instead, whose short CTAs
+//      share the SMs with the packed launches of smaller requests.
+// Transfers up to kSmallCopy bytes use their own copy streams in each
+// direction, so small requests never queue behind a large transfer.  Up to
+// max_inflight launches run at once.  Twiddle tables come from the
+// process-wide cache and stay resident.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -38,6 +41,7 @@ namespace {
 
 using Clock = std::chrono::steady_clock;
 constexpr int kBackfill = 16;
+constexpr uint64_t kSmallCopy = (uint64_t)16 << 20;  // transfers up to this size take the express streams
 constexpr size_t kSlotJobs = 8192;
 constexpr size_t kSlotWork = (size_t)8 << 20;
 
@@ -134,7 +138,8 @@ struct gsn_server {
   gsn::Arena arena;
   gsn_server_config cfg{};
   std::vector<gsn::Slot> slots;
-  cudaStream_t copy_in = nullptr, copy_out = nullptr;
+  // transfers of at most kSmallCopy bytes use their own streams, so they never queue behind large ones
+  cudaStream_t copy_in = nullptr, copy_out = nullptr, copy_in_small = nullptr, copy_out_small = nullptr;
   std::mutex mu;
   std::condition_variable cv;       // wakes the scheduler
   std::condition_variable done_cv;  // wakes waiters
@@ -192,8 +197,9 @@ void finish(gsn_server* S, Req& q, State st, int rc) {
 
 bool try_admit(gsn_server* S, Req& q) {
   const uint64_t db = elem_bytes(q.F, q.r.log_n);
-  const Plan p = plan_for(*q.F, (int)q.r.log_n, /*batched=*/true);
-  const uint64_t sb = job_scratch_bytes(*q.F, p);
+  // scratch for the packed launch's plan or the per-pass plan, whichever runs it
+  const uint64_t sb = std::max(job_scratch_bytes(*q.F, plan_for(*q.F, (int)q.r.log_n, /*batched=*/true)),
+                               job_scratch_bytes(*q.F, plan_for(*q.F, (int)q.r.log_n)));
   uint64_t doff = 0, soff = 0;
   if (!S->arena.alloc(db, &doff)) return false;
   if (sb && !S->arena.alloc(sb, &soff)) {
@@ -206,8 +212,9 @@ bool try_admit(gsn_server* S, Req& q) {
   q.scratch_off = soff;
   q.scratch_bytes = sb;
   q.has_scratch = sb != 0;
-  cudaError_t e = cudaMemcpyAsync(dptr(S, doff), q.r.host_in, db, cudaMemcpyHostToDevice, S->copy_in);
-  if (e == cudaSuccess) e = cudaEventRecord(q.ev, S->copy_in);
+  cudaStream_t cs = db <= kSmallCopy ? S->copy_in_small : S->copy_in;
+  cudaError_t e = cudaMemcpyAsync(dptr(S, doff), q.r.host_in, db, cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess) e = cudaEventRecord(q.ev, cs);
   if (e != cudaSuccess) {
     finish(S, q, kFailed, cuda_fail(e, "request upload"));
     return true;
@@ -226,6 +233,38 @@ int occupancy(gsn_server* S, const FieldOps* F, int block, size_t smem) {
   return v;
 }
 
+// A lone request whose work exceeds the launch cap: its passes run as ordinary per-pass launches on the
+// slot's stream.  Their CTAs each take one tile and exit, so packed launches of later, smaller requests on
+// the other slots get SMs as tiles finish, instead of waiting for a persistent launch that holds every SM
+// until its last tile.  (Giving the packed launches a higher stream priority starved these requests:
+// their compute phase stretched to ~30x its standalone time under a steady stream of small launches.)
+void launch_single(gsn_server* S, Slot& sl, uint64_t id) {
+  Req& q = S->reqs[id];
+  Tables T;
+  int rc = resolve_tables(*q.F, q.r.log_n, nullptr, q.r.dir, q.has_shift ? q.shift : nullptr, &T, sl.stream);
+  const Plan plan = plan_for(*q.F, (int)q.r.log_n);
+  if (!rc && plan.kernel == kKernelP32) rc = resolve_p32_tables(*q.F, plan, &T);
+  uint32_t* scratch = q.has_scratch ? dptr(S, q.scratch_off) : nullptr;
+  if (!rc && plan.npass > 1 && !scratch) rc = set_error(GSN_ERR_STATE, "request admitted without scratch");
+  if (!rc) rc = enqueue_ntt(*q.F, plan, T, dptr(S, q.data_off), scratch, sl.stream);
+  cudaError_t e = cudaSuccess;
+  if (!rc) {
+    *sl.status_host = 0;  // no bounded device waits on this path
+    e = cudaEventRecord(sl.done, sl.stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "serving launch");
+  }
+  if (rc) {
+    finish(S, q, kFailed, rc);
+    return;
+  }
+  ++S->launches;
+  q.st = kRunning;
+  q.t_launch = Clock::now();
+  sl.reqs = {id};
+  sl.busy = true;
+  if (S->inflight++ == 0) S->busy_since = Clock::now();
+}
+
 // Pack ready requests of one field into a launch on slot `si`.
 void launch(gsn_server* S, int si) {
   Slot& sl = S->slots[si];
@@ -233,6 +272,15 @@ void launch(gsn_server* S, int si) {
   const FieldOps* F = S->reqs[S->ready.front()].F;
   const size_t cap = S->cfg.max_batch_jobs > 0 ? (size_t)S->cfg.max_batch_jobs : 4096;
   const double work_cap = S->cfg.max_launch_work ? (double)S->cfg.max_launch_work : 4e10;
+  {
+    const Req& q0 = S->reqs[S->ready.front()];
+    if (request_work(q0.F, q0.r.log_n) > work_cap) {
+      const uint64_t id = S->ready.front();
+      S->ready.pop_front();
+      launch_single(S, sl, id);
+      return;
+    }
+  }
   std::vector<uint64_t> ids;
   std::deque<uint64_t> keep;
   double work = 0;
@@ -321,10 +369,11 @@ void retire(gsn_server* S, Slot& sl) {
       continue;
     }
     if (q.r.host_out) {
-      cudaError_t e = cudaStreamWaitEvent(S->copy_out, sl.done, 0);
+      cudaStream_t cs = q.data_bytes <= kSmallCopy ? S->copy_out_small : S->copy_out;
+      cudaError_t e = cudaStreamWaitEvent(cs, sl.done, 0);
       if (e == cudaSuccess)
-        e = cudaMemcpyAsync(q.r.host_out, dptr(S, q.data_off), q.data_bytes, cudaMemcpyDeviceToHost, S->copy_out);
-      if (e == cudaSuccess) e = cudaEventRecord(q.ev, S->copy_out);
+        e = cudaMemcpyAsync(q.r.host_out, dptr(S, q.data_off), q.data_bytes, cudaMemcpyDeviceToHost, cs);
+      if (e == cudaSuccess) e = cudaEventRecord(q.ev, cs);
       if (e != cudaSuccess) {
         finish(S, q, kFailed, cuda_fail(e, "result download"));
         continue;
@@ -427,6 +476,8 @@ int gsn_server_create(const gsn_server_config* cfg, gsn_server** out) {
   cudaDeviceGetAttribute(&S->sms, cudaDevAttrMultiProcessorCount, dev);
   cudaError_t e = cudaStreamCreateWithFlags(&S->copy_in, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->copy_out, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->copy_in_small, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&S->copy_out_small, cudaStreamNonBlocking);
   S->slots.resize(cfg->max_inflight);
   for (Slot& sl : S->slots) {
     if (e != cudaSuccess) break;
@@ -578,8 +629,8 @@ int gsn_server_destroy(gsn_server* S) {
     if (sl.work_host) cudaFreeHost(sl.work_host);
     if (sl.status_host) cudaFreeHost(sl.status_host);
   }
-  if (S->copy_in) cudaStreamDestroy(S->copy_in);
-  if (S->copy_out) cudaStreamDestroy(S->copy_out);
+  for (cudaStream_t cs : {S->copy_in, S->copy_out, S->copy_in_small, S->copy_out_small})
+    if (cs) cudaStreamDestroy(cs);
   S->arena.destroy();
   delete S;
   return GSN_OK;

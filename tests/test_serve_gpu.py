@@ -54,6 +54,35 @@ def test_results_match_plain_path_alone_and_in_mix(gsn, cuda_device):
         srv.close()
 
 
+def test_requests_over_the_work_cap_run_per_pass(gsn, cuda_device):
+    """With max_launch_work = 1 every request exceeds the cap and runs alone through the per-pass kernels
+    (forward, inverse and coset forward, both fields, resident and copied-out results); mixed with a
+    second server's packed launches, results equal the plain path."""
+    from gpusnarks_gb300.serve import Server
+    reqs = _requests(gsn, 24, 11, lo=8, hi=16)
+    want = [_plain(gsn, f, x, d) for f, k, d, x in reqs]
+    lone = Server(1 << 31, max_inflight=2, max_launch_work=1)
+    packed = Server(1 << 31, max_inflight=2)
+    try:
+        outs = [np.empty_like(x) for _, _, _, x in reqs]
+        ids = []
+        for i, ((f, k, d, x), o) in enumerate(zip(reqs, outs)):
+            srv = lone if i % 3 else packed
+            ids.append((srv, srv.submit(f, x, d, host_out=None if i % 4 == 0 else o)))
+        for i, (srv, rid) in enumerate(ids):
+            srv.wait(rid)
+            if i % 4 == 0:
+                srv.fetch(rid, outs[i])
+            srv.release(rid)
+        for o, w in zip(outs, want):
+            assert np.array_equal(o, w)
+        st = lone.stats()
+        assert st["failed"] == 0 and st["launches"] == st["completed"]  # one launch per request
+    finally:
+        lone.close()
+        packed.close()
+
+
 def test_budget_admission_and_resident_results(gsn, cuda_device):
     from gpusnarks_gb300.serve import Server
     f = gsn.MNT4_753
