@@ -154,6 +154,7 @@ struct gsn_server {
   gsn::Clock::time_point busy_since;
   int sms = 0;
   std::map<std::tuple<int, int, size_t>, int> occ;  // (field, block, smem) -> blocks per SM
+  double step_max_s[5] = {0, 0, 0, 0, 0};            // longest admission / upload / retire / download / launch step
 };
 
 namespace gsn {
@@ -393,6 +394,12 @@ void scheduler(gsn_server* S) {
   std::unique_lock<std::mutex> lk(S->mu);
   while (!S->stop) {
     bool progressed = false;
+    Clock::time_point tick = Clock::now();
+    auto step_done = [&](int k) {  // longest time each step of an iteration has taken
+      const Clock::time_point now = Clock::now();
+      S->step_max_s[k] = std::max(S->step_max_s[k], seconds(now - tick));
+      tick = now;
+    };
     // 1. admission (arrival order, bounded backfill)
     {
       std::deque<uint64_t> still;
@@ -411,6 +418,7 @@ void scheduler(gsn_server* S) {
       }
       S->pending.swap(still);
     }
+    step_done(0);
     // 2. uploads finished
     for (auto it = S->copyin.begin(); it != S->copyin.end();) {
       if (cudaEventQuery(S->reqs[*it].ev) == cudaSuccess) {
@@ -423,6 +431,7 @@ void scheduler(gsn_server* S) {
         ++it;
       }
     }
+    step_done(1);
     // 3. launches finished
     for (Slot& sl : S->slots) {
       if (sl.busy && cudaEventQuery(sl.done) == cudaSuccess) {
@@ -430,6 +439,7 @@ void scheduler(gsn_server* S) {
         progressed = true;
       }
     }
+    step_done(2);
     // 4. downloads finished
     for (auto it = S->copyout.begin(); it != S->copyout.end();) {
       Req& q = S->reqs[*it];
@@ -442,6 +452,7 @@ void scheduler(gsn_server* S) {
         ++it;
       }
     }
+    step_done(3);
     // 5. new launches while slots are free
     for (size_t si = 0; si < S->slots.size() && !S->ready.empty(); ++si) {
       if (!S->slots[si].busy) {
@@ -449,6 +460,7 @@ void scheduler(gsn_server* S) {
         progressed = true;
       }
     }
+    step_done(4);
     if (!progressed) S->cv.wait_for(lk, std::chrono::microseconds(20));
   }
 }
@@ -604,6 +616,7 @@ int gsn_server_get_stats(gsn_server* S, gsn_server_stats* st) {
   st->device_bytes_in_use = S->arena.used;
   st->device_bytes_peak = S->arena.peak;
   st->busy_s = S->busy_s + (S->inflight ? seconds(Clock::now() - S->busy_since) : 0.0);
+  for (int k = 0; k < 5; ++k) st->step_max_s[k] = S->step_max_s[k];
   return GSN_OK;
 }
 

@@ -29,7 +29,8 @@ class TraceEntry(ctypes.Structure):
 class ServerStats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("failed", ctypes.c_uint64),
                 ("launches", ctypes.c_uint64), ("device_bytes_in_use", ctypes.c_uint64),
-                ("device_bytes_peak", ctypes.c_uint64), ("busy_s", ctypes.c_double)]
+                ("device_bytes_peak", ctypes.c_uint64), ("busy_s", ctypes.c_double),
+                ("step_max_s", ctypes.c_double * 5)]
 
 
 _SIGS = [
@@ -101,7 +102,9 @@ class Server:
     def stats(self) -> dict:
         st = ServerStats()
         check(self.lib.gsn_server_get_stats(self.h, ctypes.byref(st)))
-        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+        out = {k: getattr(st, k) for k, _ in ServerStats._fields_}
+        out["step_max_s"] = list(st.step_max_s)
+        return out
 
     def run_trace(self, entries, phases: bool = False):
         """Replay (arrival, Request) entries.  Returns (latencies, makespan), and with phases=True also an
@@ -182,6 +185,8 @@ def bench_serving(g, torch, *, seconds: float = 1.0, rate: float = 2000.0, budge
             "throughput_req_s": round(len(trace) / makespan, 1),
             "throughput_Melem_s": round(elements / makespan / 1e6, 2),
             "launches": st["launches"], "device_bytes_peak": st["device_bytes_peak"],
+            "scheduler_step_max_ms": {k: round(v * 1e3, 3) for k, v in
+                                      zip(("admit", "uploads", "retire", "downloads", "launch"), st["step_max_s"])},
             "phase_ms_p50": {k: round(float(np.percentile(ph[:, i], 50)) * 1e3, 3) for i, k in enumerate(PHASES)},
             "phase_ms_p99": {k: round(float(np.percentile(ph[:, i], 99)) * 1e3, 3) for i, k in enumerate(PHASES)},
             "p99_request_phases_ms": {k: round(float(ph[int(np.argsort(lat)[int(0.99 * (len(lat) - 1))]), i]) * 1e3, 3)

@@ -243,6 +243,10 @@ typedef struct gsn_server_stats {
   uint64_t submitted, completed, failed, launches;
   uint64_t device_bytes_in_use, device_bytes_peak;
   double busy_s; /* wall time with at least one launch in flight */
+  /* longest single pass of each scheduler step, seconds: admission,
+   * upload completions, launch completions, download completions, new
+   * launches (the scheduler holds the server lock throughout) */
+  double step_max_s[5];
 } gsn_server_stats;
 
 int gsn_server_create(const gsn_server_config* cfg, gsn_server** out);
