@@ -85,6 +85,35 @@ def best_fft(a: np.ndarray, omg=None, *, field=None, direction=FORWARD, shift=No
     return a
 
 
+def best_fft_many(arrays, omg=None, *, field=None, direction=FORWARD, shift=None):
+    """``best_fft`` on several host arrays of one size, each in place, with the copies of neighbouring arrays
+    overlapping each transform (gsn_ntt_host_batch).  ``arrays``: C-contiguous numpy uint32 arrays, or
+    integer addresses of host buffers (e.g. from host_buffer) with ``field`` and the size given by ``log_n``
+    through a (address, log_n) tuple.  Returns the list."""
+    items = list(arrays)
+    if not items:
+        return items
+    ptrs, sizes = [], set()
+    for a in items:
+        if isinstance(a, tuple):
+            ptrs.append(int(a[0]))
+            sizes.add(int(a[1]))
+            continue
+        if not isinstance(a, np.ndarray) or a.dtype != np.uint32 or not a.flags.c_contiguous:
+            raise TypeError("best_fft_many expects C-contiguous numpy uint32 arrays")
+        if field is None:
+            field = {1: P32, 8: BLS12_381, 24: MNT4_753}[1 if a.ndim == 1 else a.shape[1]]
+        ptrs.append(a.ctypes.data)
+        sizes.add(_log2_exact(a.size // field_of(field).limbs))
+    if field is None or len(sizes) != 1:
+        raise ValueError("best_fft_many needs one field and one size for all arrays")
+    f = field_of(field)
+    arr = (ctypes.c_void_p * len(ptrs))(*ptrs)
+    check(load().gsn_ntt_host_batch(f.fid, arr, len(ptrs), sizes.pop(), u32p(_limbs(f, omg)), int(direction),
+                                    u32p(_limbs(f, shift))))
+    return items
+
+
 def _stream_handle(stream):
     if stream is None:
         import torch

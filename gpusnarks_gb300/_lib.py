@@ -40,6 +40,8 @@ _SIGNATURES = [
     ("gsn_ntt_scratch", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint32, _u32p, ctypes.c_int,
                                        _u32p, ctypes.c_void_p, ctypes.c_void_p]),
     ("gsn_ntt_host", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint32, _u32p, ctypes.c_int, _u32p]),
+    ("gsn_ntt_host_batch", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t,
+                                          ctypes.c_uint32, _u32p, ctypes.c_int, _u32p]),
     ("gsn_ntt_noalloc", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int,
                                        ctypes.c_void_p]),
     ("gsn_prepare", ctypes.c_int, [ctypes.c_int, ctypes.c_uint32, _u32p]),

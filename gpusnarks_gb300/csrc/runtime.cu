@@ -655,6 +655,68 @@ int gsn_ntt_host(int field, uint32_t* data, uint32_t log_n, const uint32_t* omeg
   return GSN_OK;
 }
 
+int gsn_ntt_host_batch(int field, uint32_t* const* data, size_t count, uint32_t log_n, const uint32_t* omega,
+                       int dir, const uint32_t* shift) {
+  const FieldOps* F = field_ops(field);
+  if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);
+  if (count && !data) return set_error(GSN_ERR_ARG, "null array list");
+  for (size_t i = 0; i < count; ++i)
+    if (!data[i]) return set_error(GSN_ERR_ARG, "null data pointer at %zu", i);
+  if ((int)log_n > std::min(F->max_log_n, F->two_adicity))
+    return set_error(GSN_ERR_SIZE, "log_n=%u exceeds the limit for field %d", log_n, field);
+  if (count == 0) return GSN_OK;
+  std::lock_guard<std::mutex> g(g_host_mu);
+  // three device buffers in rotation; copy-in, transform and copy-out on their own streams, ordered by
+  // events, so array i+1 uploads and array i-1 downloads while array i is transformed
+  constexpr int kBufs = 3;
+  static cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
+  static DevBuf bufs[kBufs];
+  static cudaEvent_t ev_in[kBufs], ev_comp[kBufs], ev_out[kBufs];
+  if (!s_in) {
+    GSN_CUDA(cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking));
+    GSN_CUDA(cudaStreamCreateWithFlags(&s_comp, cudaStreamNonBlocking));
+    GSN_CUDA(cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking));
+    for (int b = 0; b < kBufs; ++b) {
+      GSN_CUDA(cudaEventCreateWithFlags(&ev_in[b], cudaEventDisableTiming));
+      GSN_CUDA(cudaEventCreateWithFlags(&ev_comp[b], cudaEventDisableTiming));
+      GSN_CUDA(cudaEventCreateWithFlags(&ev_out[b], cudaEventDisableTiming));
+    }
+  }
+  const size_t bytes = ((size_t)1 << log_n) * F->limbs * sizeof(uint32_t);
+  for (DevBuf& b : bufs) {
+    if (b.bytes < bytes) {
+      GSN_CUDA(cudaStreamSynchronize(s_out));  // earlier batches are done with it
+      dev_free(b.p);
+      b.p = nullptr;
+      b.bytes = 0;
+      int rc = dev_alloc(&b.p, bytes);
+      if (rc) return rc;
+      b.bytes = bytes;
+    }
+  }
+  for (size_t i = 0; i < count; ++i) {
+    const int b = (int)(i % kBufs);
+    uint32_t* dev = static_cast<uint32_t*>(bufs[b].p);
+    if (i >= kBufs) GSN_CUDA(cudaStreamWaitEvent(s_in, ev_out[b], 0));  // array i-3 has left this buffer
+    GSN_CUDA(cudaMemcpyAsync(dev, data[i], bytes, cudaMemcpyHostToDevice, s_in));
+    GSN_CUDA(cudaEventRecord(ev_in[b], s_in));
+    GSN_CUDA(cudaStreamWaitEvent(s_comp, ev_in[b], 0));
+    int rc = ntt_impl(field, dev, log_n, omega, dir, shift, nullptr, s_comp);
+    if (rc) {
+      cudaStreamSynchronize(s_in);
+      cudaStreamSynchronize(s_comp);
+      cudaStreamSynchronize(s_out);
+      return rc;
+    }
+    GSN_CUDA(cudaEventRecord(ev_comp[b], s_comp));
+    GSN_CUDA(cudaStreamWaitEvent(s_out, ev_comp[b], 0));
+    GSN_CUDA(cudaMemcpyAsync(data[i], dev, bytes, cudaMemcpyDeviceToHost, s_out));
+    GSN_CUDA(cudaEventRecord(ev_out[b], s_out));
+  }
+  GSN_CUDA(cudaStreamSynchronize(s_out));
+  return GSN_OK;
+}
+
 int gsn_prepare(int field, uint32_t log_n, const uint32_t* omega) {
   const FieldOps* F = field_ops(field);
   if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);

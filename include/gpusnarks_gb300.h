@@ -108,6 +108,17 @@ int gsn_ntt_noalloc(int field, uint32_t* data, uint32_t log_n, int dir, void* st
 int gsn_ntt_host(int field, uint32_t* data, uint32_t log_n, const uint32_t* omega, int dir,
                  const uint32_t* shift);
 
+/* best_fft over many host arrays (no counterpart in the reference, whose
+ * callers loop over best_fft): data[0..count) are distinct host arrays of
+ * 2^log_n elements each, all transformed in place with the same root,
+ * direction and shift; returns when every result is back.  Copy-in of array
+ * i+1 and copy-out of array i-1 overlap the transform of array i (three
+ * device buffers, separate copy and compute streams), so with page-locked
+ * arrays the throughput approaches the transform's own rather than the sum
+ * of both copies and the transform. */
+int gsn_ntt_host_batch(int field, uint32_t* const* data, size_t count, uint32_t log_n, const uint32_t* omega,
+                       int dir, const uint32_t* shift);
+
 /* Build and cache the twiddle table for (field, log_n, omega). */
 int gsn_prepare(int field, uint32_t log_n, const uint32_t* omega);
 

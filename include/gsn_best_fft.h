@@ -78,6 +78,24 @@ void transform(std::vector<FieldT>& a, const FieldT* omg, int dir, const FieldT*
                      reinterpret_cast<const uint32_t*>(omg), dir, reinterpret_cast<const uint32_t*>(shift)));
 }
 
+// best_fft on several vectors of one size, in place; the copies of neighbouring vectors overlap each
+// transform (gsn_ntt_host_batch).  For callers that would otherwise loop over best_fft.
+template <typename FieldT>
+void best_fft_many(std::vector<std::vector<FieldT>*> vs, const FieldT& omg, int dir = GSN_FORWARD) {
+  static_assert(std::is_trivially_copyable<FieldT>::value, "FieldT must be trivially copyable");
+  using T = field_traits<FieldT>;
+  static_assert(sizeof(FieldT) == sizeof(uint32_t) * T::limbs, "FieldT must be uint32_t im_rep[LIMBS]");
+  if (vs.empty()) return;
+  const uint32_t log_n = log2_exact(vs[0]->size());
+  std::vector<uint32_t*> ptrs;
+  for (std::vector<FieldT>* v : vs) {
+    if (v->size() != vs[0]->size()) throw Error(GSN_ERR_SIZE, "best_fft_many: vectors differ in size");
+    ptrs.push_back(reinterpret_cast<uint32_t*>(v->data()));
+  }
+  check(gsn_ntt_host_batch(T::id, ptrs.data(), ptrs.size(), log_n, reinterpret_cast<const uint32_t*>(&omg), dir,
+                           nullptr));
+}
+
 }  // namespace gsn
 
 // The reference's entry point (cuda/fft_kernel.h:24-25).

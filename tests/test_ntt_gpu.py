@@ -157,6 +157,49 @@ def test_host_path_pinned(gsn, cuda_device):
             gsn.free_host_buffer(buf)
 
 
+@pytest.mark.parametrize("fname,log_n,count", [("mnt4753_fr", 12, 7), ("bls12_381_fr", 14, 5),
+                                               ("p32", 18, 4), ("mnt4753_fr", 15, 2)])
+def test_host_batch_pipelined(gsn, cuda_device, fname, log_n, count):
+    """gsn_ntt_host_batch: several host arrays through the copy/compute pipeline, each equal to its own
+    oracle transform; pageable numpy arrays and page-locked buffers; forward, then inverse back."""
+    import ctypes
+    f = gsn.FIELDS[fname]
+    xs = [f.random_array(1 << log_n, seed=SEED + 400 + 13 * i + log_n) for i in range(count)]
+    work = [x.copy() for x in xs]
+    gsn.best_fft_many(work, field=f)
+    for w, x in zip(work, xs):
+        assert np.array_equal(w, O.ntt(f.fid, x).reshape(x.shape))
+    gsn.best_fft_many(work, field=f, direction=gsn.INVERSE)
+    for w, x in zip(work, xs):
+        assert np.array_equal(w, x)
+    bufs = [gsn.host_buffer(x.nbytes) for x in xs]
+    try:
+        views = []
+        for b, x in zip(bufs, xs):
+            v = np.ctypeslib.as_array(ctypes.cast(b, ctypes.POINTER(ctypes.c_uint32)), shape=(x.size,))
+            v[:] = x.reshape(-1)
+            views.append(v)
+        gsn.best_fft_many([(b.value, log_n) for b in bufs], field=f, direction=gsn.COSET_FORWARD)
+        for v, x in zip(views, xs):
+            assert np.array_equal(v.reshape(x.shape), O.coset_ntt(f.fid, x, f.generator).reshape(x.shape))
+    finally:
+        for b in bufs:
+            gsn.free_host_buffer(b)
+
+
+def test_host_batch_errors(gsn, cuda_device):
+    import ctypes
+    lib = gsn.load()
+    assert lib.gsn_ntt_host_batch(1, None, 0, 4, None, 0, None) == 0
+    assert lib.gsn_ntt_host_batch(1, None, 2, 4, None, 0, None) == 1
+    arr = (ctypes.c_void_p * 2)(None, None)
+    assert lib.gsn_ntt_host_batch(1, arr, 2, 4, None, 0, None) == 1
+    x = gsn.BLS12_381.random_array(16, seed=3)
+    arr = (ctypes.c_void_p * 1)(x.ctypes.data)
+    assert lib.gsn_ntt_host_batch(1, arr, 1, 40, None, 0, None) == 3
+    assert lib.gsn_ntt_host_batch(9, arr, 1, 4, None, 0, None) == 2
+
+
 @pytest.mark.parametrize("log_n", [12, 18, 22])
 def test_p32_four_byte_aligned_arrays(gsn, cuda_device, log_n):
     """p32 data and scratch only 4-byte aligned (offset by one element) take the generic pass instead of
