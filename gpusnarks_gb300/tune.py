@@ -4,9 +4,10 @@
 
 Times the candidate plans of gsn_autotune (single transforms) and
 gsn_autotune_batch (inside the persistent batched kernel) for each field over
-the sizes the workloads use (p32 2^8..2^28, BLS12-381 2^8..2^22, MNT4-753
-2^6..2^22) and saves the fastest per (field, log n, mode).  gpusnarks_gb300
-loads the committed table at start-up.
+every supported size for single transforms (p32 2^8..2^28, BLS12-381
+2^8..2^26, MNT4-753 2^6..2^24) and up to 2^22 inside the batched kernel, and
+saves the fastest per (field, log n, mode).  gpusnarks_gb300 loads the
+committed table at start-up.
 """
 from __future__ import annotations
 
@@ -26,7 +27,7 @@ def main() -> None:
 
     import gpusnarks_gb300 as g
 
-    ranges = {"p32": (8, 28), "bls12_381_fr": (8, 22), "mnt4753_fr": (6, 22)}
+    ranges = {"p32": (8, 28), "bls12_381_fr": (8, 26), "mnt4753_fr": (6, 24)}
     batch_ranges = {"p32": (8, 22), "bls12_381_fr": (8, 22), "mnt4753_fr": (6, 22)}
     g.load()
     g.clear_tuning()
