@@ -570,6 +570,10 @@ static int quotient_impl(int field, uint32_t* a, const uint32_t* b, const uint32
 }
 
 static std::mutex g_host_mu;
+// device buffers of the host-memory entry points (gsn_ntt_host, gsn_ntt_host_batch), guarded by g_host_mu and
+// freed by gsn_release_caches
+static DevBuf g_host_single;
+static DevBuf g_host_pipe[3];
 }  // namespace gsn
 
 using namespace gsn;
@@ -632,7 +636,7 @@ int gsn_ntt_host(int field, uint32_t* data, uint32_t log_n, const uint32_t* omeg
     return set_error(GSN_ERR_SIZE, "log_n=%u exceeds the limit for field %d", log_n, field);
   std::lock_guard<std::mutex> g(g_host_mu);
   static cudaStream_t stream = nullptr;
-  static DevBuf buf;
+  DevBuf& buf = g_host_single;
   if (!stream) GSN_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   const size_t bytes = ((size_t)1 << log_n) * F->limbs * sizeof(uint32_t);
   if (buf.bytes < bytes) {
@@ -670,7 +674,7 @@ int gsn_ntt_host_batch(int field, uint32_t* const* data, size_t count, uint32_t 
   // events, so array i+1 uploads and array i-1 downloads while array i is transformed
   constexpr int kBufs = 3;
   static cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
-  static DevBuf bufs[kBufs];
+  DevBuf* const bufs = g_host_pipe;
   static cudaEvent_t ev_in[kBufs], ev_comp[kBufs], ev_out[kBufs];
   if (!s_in) {
     GSN_CUDA(cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking));
@@ -683,7 +687,8 @@ int gsn_ntt_host_batch(int field, uint32_t* const* data, size_t count, uint32_t 
     }
   }
   const size_t bytes = ((size_t)1 << log_n) * F->limbs * sizeof(uint32_t);
-  for (DevBuf& b : bufs) {
+  for (int k = 0; k < kBufs; ++k) {
+    DevBuf& b = bufs[k];
     if (b.bytes < bytes) {
       GSN_CUDA(cudaStreamSynchronize(s_out));  // earlier batches are done with it
       dev_free(b.p);
@@ -792,9 +797,15 @@ int gsn_host_free(void* ptr) {
 }
 
 int gsn_release_caches(void) {
+  std::lock_guard<std::mutex> gh(g_host_mu);  // same order as the host entry points: host lock, then cache
   TableCache& C = cache();
   std::lock_guard<std::mutex> g(C.mu);
   GSN_CUDA(cudaDeviceSynchronize());
+  for (DevBuf* b : {&g_host_single, &g_host_pipe[0], &g_host_pipe[1], &g_host_pipe[2]}) {
+    dev_free(b->p);
+    b->p = nullptr;
+    b->bytes = 0;
+  }
   for (auto& kv : C.powers) dev_free(kv.second.p);
   C.powers.clear();
   for (auto& kv : C.scratch) dev_free(kv.second.p);
