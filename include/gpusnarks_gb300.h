@@ -304,7 +304,10 @@ int gsn_fill_random(int field, uint32_t* data, uint64_t n, uint64_t seed, void* 
 int gsn_synchronize(void* stream);
 int gsn_host_alloc(void** ptr, size_t bytes);  /* pinned host memory */
 int gsn_host_free(void* ptr);
-int gsn_release_caches(void);                  /* free twiddle tables and scratch */
+/* Free twiddle tables, scratch and the host-path buffers (they are rebuilt on
+ * next use).  Synchronises the device first.  gsn_batch objects and servers
+ * hold table pointers: destroy them before calling this. */
+int gsn_release_caches(void);
 /* number of NTT-path kernel launches issued by this library so far */
 uint64_t gsn_kernel_launch_count(void);
 

@@ -187,6 +187,25 @@ def test_host_batch_pipelined(gsn, cuda_device, fname, log_n, count):
             gsn.free_host_buffer(b)
 
 
+def test_release_caches_then_reuse(gsn, cuda_device):
+    """gsn_release_caches frees tables, scratch and the host-path buffers; every path rebuilds what it needs
+    on the next call and still matches the oracle."""
+    f = gsn.MNT4_753
+    x = f.random_array(1 << 11, seed=SEED + 77)
+    a = x.copy()
+    gsn.best_fft(a, None)
+    gsn.best_fft_many([a.copy(), a.copy()], field=f)
+    gsn._lib.check(gsn.load().gsn_release_caches())
+    b, c = x.copy(), x.copy()
+    gsn.best_fft(b, None)
+    gsn.best_fft_many([c], field=f)
+    d = gsn.to_device(x)
+    gsn.ntt(f, d)
+    want = O.ntt(f.fid, x).reshape(x.shape)
+    for got in (b, c, gsn.to_host(d).reshape(x.shape)):
+        assert np.array_equal(got, want)
+
+
 def test_host_batch_errors(gsn, cuda_device):
     import ctypes
     lib = gsn.load()
