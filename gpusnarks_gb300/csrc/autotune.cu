@@ -42,6 +42,21 @@ std::vector<Plan> candidates(const FieldOps& F, int log_n) {
         if (F.limbs == 24 && mb > 256) continue;
         add(make_plan(F, log_n, max_r, tj, mb));
       }
+  if (F.limbs > 1) {
+    // uneven two- and three-pass splits (stage counts, tile shapes and waves differ per pass)
+    const int lo = 4;
+    for (int a = lo; a <= max_r_hi; ++a)
+      for (int b = lo; b <= max_r_hi; ++b) {
+        const int c = log_n - a - b;
+        const int two[2] = {a, log_n - a};
+        const int three[3] = {a, b, c};
+        for (int tj = 0; tj <= j_hi; ++tj)
+          for (int mb : {64, 128, 256}) {
+            if (b == lo && log_n - a >= lo && log_n - a <= max_r_hi) add(make_split_plan(F, log_n, two, 2, tj, mb));
+            if (c >= lo && c <= max_r_hi) add(make_split_plan(F, log_n, three, 3, tj, mb));
+          }
+      }
+  }
   if (F.id == GSN_P32 && log_n >= 8) {
     for (int max_r = 7; max_r <= 14; ++max_r)
       for (int lj = 2; lj <= 3; ++lj)

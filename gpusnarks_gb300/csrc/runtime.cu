@@ -120,13 +120,8 @@ bool plan_valid(const FieldOps& F, const Plan& p) {
   return true;
 }
 
-Plan make_plan(const FieldOps& F, int log_n, int max_r, int target_j, int max_block) {
-  Plan p;
-  p.log_n = log_n;
-  p.npass = std::max(1, (log_n + max_r - 1) / max_r);
-  if (p.npass > kMaxPasses) p.npass = kMaxPasses;
-  const int base = log_n / p.npass, extra = log_n % p.npass;
-  for (int i = 0; i < p.npass; ++i) p.radix_log[i] = base + (i < extra ? 1 : 0);
+// Tile widths and threads per pass for a plan whose pass radices are set.
+static void fill_tiles(Plan& p, int target_j, int max_block) {
   for (int i = 0; i < p.npass; ++i) {
     const bool last = i == p.npass - 1;
     int inner = 0;
@@ -138,6 +133,26 @@ Plan make_plan(const FieldOps& F, int log_n, int max_r, int target_j, int max_bl
     while (blk < max_block && blk < work) blk *= 2;
     p.block[i] = blk;
   }
+}
+
+Plan make_plan(const FieldOps& F, int log_n, int max_r, int target_j, int max_block) {
+  Plan p;
+  p.log_n = log_n;
+  p.npass = std::max(1, (log_n + max_r - 1) / max_r);
+  if (p.npass > kMaxPasses) p.npass = kMaxPasses;
+  const int base = log_n / p.npass, extra = log_n % p.npass;
+  for (int i = 0; i < p.npass; ++i) p.radix_log[i] = base + (i < extra ? 1 : 0);
+  fill_tiles(p, target_j, max_block);
+  (void)F;
+  return p;
+}
+
+Plan make_split_plan(const FieldOps& F, int log_n, const int* radix_log, int npass, int target_j, int max_block) {
+  Plan p;
+  p.log_n = log_n;
+  p.npass = std::min(npass, kMaxPasses);
+  for (int i = 0; i < p.npass; ++i) p.radix_log[i] = radix_log[i];
+  fill_tiles(p, target_j, max_block);
   (void)F;
   return p;
 }

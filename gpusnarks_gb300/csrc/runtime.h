@@ -49,6 +49,8 @@ Plan plan_for(const FieldOps& F, int log_n, bool batched = false);
 Plan make_p32_plan(int log_n, int max_r, int log_j, int e_log);
 // Heuristic plan with explicit limits (used by the autotuner's candidate set).
 Plan make_plan(const FieldOps& F, int log_n, int max_r, int target_j, int max_block);
+// The same tile widths and threads for an explicit split of log_n into npass radices.
+Plan make_split_plan(const FieldOps& F, int log_n, const int* radix_log, int npass, int target_j, int max_block);
 bool plan_valid(const FieldOps& F, const Plan& p);
 size_t plan_smem_bytes(const FieldOps& F, const Plan& p, int pass);
 // mode 0: plans for single transforms; mode 1: plans for the batched kernel
