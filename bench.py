@@ -135,6 +135,76 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+class NvmlSampler:
+    """Reads the SM clock and the clock-event (throttle) reasons through NVML every ~2 ms in a thread, so
+    even a timed region of a few milliseconds is covered.  Read-only queries; raises on any NVML error so
+    the caller can fall back to nvidia-smi."""
+
+    SW_POWER_CAP, HW_SLOWDOWN, SW_THERMAL, HW_THERMAL = 0x4, 0x8, 0x20, 0x40
+
+    def __init__(self, torch, index: int):
+        self.lib = ctypes.CDLL("libnvidia-ml.so.1")
+        self.samples: list[tuple[int, int]] = []
+        self.stop = False
+        if self.lib.nvmlInit_v2() != 0:
+            raise RuntimeError("nvmlInit failed")
+        try:
+            self.h = ctypes.c_void_p()
+            uuid = "GPU-" + str(torch.cuda.get_device_properties(index).uuid)
+            if self.lib.nvmlDeviceGetHandleByUUID(uuid.encode(), ctypes.byref(self.h)) != 0:
+                raise RuntimeError("no NVML handle for " + uuid)
+            self.reasons_fn = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+            mx = ctypes.c_uint()
+            if self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, ctypes.byref(mx)) != 0:  # 1 = NVML_CLOCK_SM
+                raise RuntimeError("nvmlDeviceGetMaxClockInfo failed")
+            self.max_mhz = mx.value
+            self._sample()
+            if not self.samples:
+                raise RuntimeError("NVML clock query failed")
+        except Exception:
+            self.lib.nvmlShutdown()
+            raise
+
+    def _sample(self):
+        clk, rs = ctypes.c_uint(), ctypes.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.h, 1, ctypes.byref(clk)) == 0 and \
+                self.reasons_fn(self.h, ctypes.byref(rs)) == 0:
+            self.samples.append((clk.value, rs.value))
+
+    def _run(self):
+        while not self.stop:
+            self._sample()
+            time.sleep(0.002)
+
+    def __enter__(self):
+        self.samples.clear()
+        self.thread = threading.Thread(target=self._run, daemon=True)
+        self.thread.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop = True
+        self.thread.join()
+        self.lib.nvmlShutdown()
+
+    def summary(self) -> dict:
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": self.max_mhz, "reasons": [], "samples": 0, "source": "nvml"}
+        names = {self.SW_POWER_CAP: "sw_power_cap", self.HW_SLOWDOWN: "hw_slowdown",
+                 self.SW_THERMAL: "sw_thermal_slowdown", self.HW_THERMAL: "hw_thermal_slowdown"}
+        reasons = sorted({nm for _, r in self.samples for bit, nm in names.items() if r & bit})
+        return {"sm_mhz": float(np.median([c for c, _ in self.samples])), "sm_max_mhz": float(self.max_mhz),
+                "reasons": reasons, "samples": len(self.samples), "source": "nvml, every ~2 ms"}
+
+
+def clock_sampler(torch, index: int):
+    try:
+        return NvmlSampler(torch, index)
+    except Exception:
+        return ClockSampler(index)
+
+
 def peaks() -> dict:
     try:
         return json.loads(PEAKS.read_text())
@@ -358,7 +428,7 @@ def run_gpu(args, rank, local, ws):
     # headline: device-resident transforms
     barrier(ws)
     torch.cuda.synchronize()
-    with ClockSampler(local) as clk:
+    with clock_sampler(torch, local) as clk:
         ts, launches = time_device_ntt(g, torch, f, log_n, args.steps, args.warmup, flush=flush)
     torch.cuda.synchronize()
     barrier(ws)
