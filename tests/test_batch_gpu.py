@@ -106,3 +106,9 @@ def test_batch_rejects_bad_jobs(gsn, cuda_device):
         Batch(f, [(d.data_ptr(), 40, 0, None, None)])
     with pytest.raises(gsn.GsnError, match="OMEGA"):
         Batch(f, [(d.data_ptr(), 4, 0, 2, None)])
+
+
+def test_batch_rejects_empty_job_list(gsn, cuda_device):
+    from gpusnarks_gb300.batch import Batch
+    with pytest.raises(gsn.GsnError, match="ARG"):
+        Batch(gsn.BLS12_381, [])

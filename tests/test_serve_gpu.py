@@ -131,3 +131,15 @@ def test_run_trace_small(gsn, cuda_device):
     assert ph.shape == (len(entries), 5)
     assert (ph[:, 1:] >= 0).all() and (ph[:, 0] > -1e-3).all()
     assert np.allclose(ph.sum(axis=1), lat, atol=1e-4)
+
+
+def test_run_trace_empty(gsn, cuda_device):
+    from gpusnarks_gb300.serve import Server
+    srv = Server(1 << 24, max_inflight=2)
+    try:
+        lat, makespan = srv.run_trace([])
+        lat2, makespan2, ph = srv.run_trace([], phases=True)
+    finally:
+        srv.close()
+    assert lat.shape == (0,) and lat2.shape == (0,) and ph.shape == (0, 5)
+    assert makespan == 0.0 and makespan2 == 0.0
