@@ -765,6 +765,7 @@ int gsn_coset_quotient(int field, uint32_t* a, const uint32_t* b, const uint32_t
 
 int gsn_qap_h(int field, uint32_t* a, uint32_t* b, uint32_t* c, uint32_t log_n, const uint32_t* shift,
               void* stream) {
+  if (!a || !b || !c) return set_error(GSN_ERR_ARG, "null data pointer");
   if (a == b || a == c || b == c) return set_error(GSN_ERR_ARG, "a, b and c must be distinct arrays");
   const cudaStream_t s = static_cast<cudaStream_t>(stream);
   uint32_t* polys[3] = {a, b, c};

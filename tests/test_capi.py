@@ -73,3 +73,42 @@ def test_bad_field_and_size_rejected_without_gpu(gsn):
     assert lib.gsn_root_of_unity(9, 4, p) == 2
     assert lib.gsn_root_of_unity(0, 31, p) == 3
     assert b"2-adicity" in lib.gsn_last_error()
+
+
+def test_entry_points_validate_before_touching_the_gpu(gsn):
+    """Every entry point checks its arguments on the host first: with no GPU here, a bad
+    argument must come back as its own error code, not as a CUDA failure."""
+    lib = gsn.load()
+    w = np.zeros(24, dtype=np.uint32)
+    w[0] = 2  # not a root of unity of any order > 2
+    wp = w.ctypes.data_as(ctypes.POINTER(ctypes.c_uint32))
+    fake = ctypes.c_void_p(0x10000)  # never dereferenced: every call below fails its checks first
+    ARG, FIELD, SIZE, OMEGA = 1, 2, 3, 4
+    cases = [
+        (lambda: lib.gsn_ntt(1, None, 4, None, 0, None, None), ARG, b"null"),
+        (lambda: lib.gsn_ntt(7, fake, 4, None, 0, None, None), FIELD, b"unknown field"),
+        (lambda: lib.gsn_ntt(1, fake, 40, None, 0, None, None), SIZE, b"exceeds"),
+        (lambda: lib.gsn_ntt(1, fake, 4, None, 9, None, None), ARG, b"direction"),
+        (lambda: lib.gsn_ntt(1, fake, 4, wp, 0, None, None), OMEGA, b"primitive"),
+        (lambda: lib.gsn_ntt(1, ctypes.c_void_p(0x10004), 4, None, 0, None, None), ARG, b"aligned"),
+        (lambda: lib.gsn_ntt_host(1, None, 4, None, 0, None), ARG, b"null"),
+        (lambda: lib.gsn_ntt_scratch(1, fake, 4, None, 0, None, None, None), ARG, b"scratch"),
+        (lambda: lib.gsn_prepare(1, 40, None), SIZE, b"exceeds"),
+        (lambda: lib.gsn_pointwise_mul(1, None, None, 16, None), ARG, b"null"),
+        (lambda: lib.gsn_convert(1, fake, 16, 7, None), ARG, b"mode"),
+        (lambda: lib.gsn_coset_quotient(1, None, None, None, 4, None, None), ARG, b"null"),
+        (lambda: lib.gsn_qap_h(1, None, None, None, 4, None, None), ARG, b"null"),
+        (lambda: lib.gsn_qap_h(1, fake, fake, ctypes.c_void_p(0x20000), 4, None, None), ARG, b"distinct"),
+        (lambda: lib.gsn_fft_ref_compat(fake, 30, wp, 3, None), SIZE, b"2^24"),
+        (lambda: lib.gsn_batch_create(1, None, 3, 0, None), ARG, b"null"),
+        (lambda: lib.gsn_server_create(None, None), ARG, b"null"),
+        (lambda: lib.gsn_server_submit(None, None, None), ARG, b"null"),
+        (lambda: lib.gsn_fill_random(1, None, 16, 1, None), ARG, b"null"),
+        (lambda: lib.gsn_autotune(9, 8, 10, 3), FIELD, b"unknown field"),
+        (lambda: lib.gsn_tuning_load(b"/nonexistent/tuning.json"), ARG, b"cannot read"),
+        (lambda: lib.gsn_plan_describe(1, 10, ctypes.create_string_buffer(4), 4), ARG, b"too small"),
+    ]
+    for i, (call, want, msg) in enumerate(cases):
+        rc = call()
+        assert rc == want and msg in lib.gsn_last_error(), (i, rc, lib.gsn_last_error())
+    assert lib.gsn_ntt_host_batch(1, None, 0, 4, None, 0, None) == 0  # nothing to do
