@@ -369,8 +369,17 @@ __device__ __forceinline__ void job_pass_args(PassArgs& A, const BatchJob& J, in
   A.tiles = (uint64_t)1 << (J.log_n - A.log_r - A.log_j);
 }
 
+// Register cap of the persistent kernel, so that it keeps about the per-pass
+// kernel's occupancy: 4 CTAs of 128 threads per SM for the 753-bit field
+// (the per-pass kernel uses 112), 32 warps per SM below.
 template <class P>
-__global__ void batch_kernel(const BatchJob* __restrict__ jobs, const uint64_t* __restrict__ work,
+constexpr int batch_max_regs() {
+  return P::N >= 16 ? 128 : 64;
+}
+
+template <class P>
+__global__ void __maxnreg__(batch_max_regs<P>())
+    batch_kernel(const BatchJob* __restrict__ jobs, const uint64_t* __restrict__ work,
                              uint64_t nwork, uint32_t* counters, uint32_t* status, long long wait_cycles) {
   extern __shared__ uint4 gsn_smem[];
   uint32_t* sm = reinterpret_cast<uint32_t*>(gsn_smem);
@@ -403,8 +412,7 @@ __global__ void batch_kernel(const BatchJob* __restrict__ jobs, const uint64_t* 
       }
     }
     __syncthreads();
-    PassArgs A = s_args;
-    ntt_tile<P>(A, tile, sm);  // ends with __syncthreads()
+    ntt_tile<P>(s_args, tile, sm);  // ends with __syncthreads(); s_args is rewritten only after it
     if (threadIdx.x == 0) {
       __threadfence();
       atomicAdd(&counters[1 + (uint64_t)job * kMaxPasses + pass], 1u);
