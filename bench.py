@@ -488,10 +488,13 @@ def run_gpu(args, rank, local, ws):
         except Exception as exc:  # report, do not hide
             extra["bls12_381_batch_4096"] = {"error": str(exc)}
         try:
-            from gpusnarks_gb300.serve import bench_serving
+            from gpusnarks_gb300.serve import LEAST_WORK_FIRST, bench_serving
             # the configured stream (2000 req/s offers more work than one GPU
             # completes, so its latency is queueing) and a sustainable rate
             extra["serving"] = bench_serving(g, torch, seconds=args.serve_seconds)
+            # the same stream, smallest transforms launched first
+            extra["serving_least_work_first"] = bench_serving(g, torch, seconds=args.serve_seconds,
+                                                              policy=LEAST_WORK_FIRST)
             # a sustainable rate; 3x the window so its p99 rests on ~12 requests rather than 4
             extra["serving_400_req_s"] = bench_serving(g, torch, seconds=3 * args.serve_seconds, rate=400.0)
         except Exception as exc:

@@ -10,7 +10,8 @@
 //   3. retires finished launches: scratch returns to the arena, results are
 //      copied out (or stay resident for a later fetch);
 //   4. while a launch slot is free, packs ready requests of one field (oldest
-//      first, up to max_batch_jobs and max_launch_work) into one persistent
+//      first, or least work first under GSN_SERVE_LEAST_WORK_FIRST, up to
+//      max_batch_jobs and max_launch_work) into one persistent
 //      launch on that slot's stream; a lone request whose work exceeds
 //      max_launch_work runs as per-pass launches instead, whose short CTAs
 //      share the SMs with the packed launches of smaller requests.
@@ -269,33 +270,42 @@ void launch_single(gsn_server* S, Slot& sl, uint64_t id) {
 // Pack ready requests of one field into a launch on slot `si`.
 void launch(gsn_server* S, int si) {
   Slot& sl = S->slots[si];
-  // oldest ready request decides the field
-  const FieldOps* F = S->reqs[S->ready.front()].F;
   const size_t cap = S->cfg.max_batch_jobs > 0 ? (size_t)S->cfg.max_batch_jobs : 4096;
   const double work_cap = S->cfg.max_launch_work ? (double)S->cfg.max_launch_work : 4e10;
-  {
-    const Req& q0 = S->reqs[S->ready.front()];
-    if (request_work(q0.F, q0.r.log_n) > work_cap) {
-      const uint64_t id = S->ready.front();
-      S->ready.pop_front();
-      launch_single(S, sl, id);
-      return;
-    }
+  auto work_of = [&](uint64_t id) {
+    const Req& q = S->reqs[id];
+    return request_work(q.F, q.r.log_n);
+  };
+  // packing order: arrival order, or least work first (ties by arrival)
+  std::vector<uint64_t> order(S->ready.begin(), S->ready.end());
+  if (S->cfg.policy == GSN_SERVE_LEAST_WORK_FIRST)
+    std::stable_sort(order.begin(), order.end(), [&](uint64_t a, uint64_t b) { return work_of(a) < work_of(b); });
+  // the leading request decides the field
+  const uint64_t lead = order.front();
+  const FieldOps* F = S->reqs[lead].F;
+  if (work_of(lead) > work_cap) {
+    S->ready.erase(std::find(S->ready.begin(), S->ready.end(), lead));
+    launch_single(S, sl, lead);
+    return;
   }
   std::vector<uint64_t> ids;
-  std::deque<uint64_t> keep;
   double work = 0;
-  for (uint64_t id : S->ready) {
+  for (uint64_t id : order) {
     const Req& q = S->reqs[id];
-    const double w = request_work(q.F, q.r.log_n);
-    // oldest first; stop packing once the launch holds work_cap (the first
-    // request always goes), so launches stay short and new arrivals start soon
+    const double w = work_of(id);
+    // stop packing once the launch holds work_cap (the leading request always
+    // goes), so launches stay short and new arrivals start soon
     if (q.F == F && ids.size() < std::min(cap, kSlotJobs) && (ids.empty() || work + w <= work_cap)) {
       ids.push_back(id);
       work += w;
-    } else {
-      keep.push_back(id);
     }
+  }
+  std::deque<uint64_t> keep;  // the rest, in arrival order
+  {
+    std::vector<uint64_t> taken(ids);
+    std::sort(taken.begin(), taken.end());
+    for (uint64_t id : S->ready)
+      if (!std::binary_search(taken.begin(), taken.end(), id)) keep.push_back(id);
   }
   std::vector<gsn_batch_job> jobs(ids.size());
   for (size_t i = 0; i < ids.size(); ++i) {
@@ -475,7 +485,9 @@ extern "C" {
 int gsn_server_create(const gsn_server_config* cfg, gsn_server** out) {
   if (!cfg || !out) return set_error(GSN_ERR_ARG, "null argument");
   *out = nullptr;
-  if (cfg->hbm_budget_bytes == 0 || cfg->max_inflight < 1) return set_error(GSN_ERR_ARG, "bad server config");
+  if (cfg->hbm_budget_bytes == 0 || cfg->max_inflight < 1 ||
+      (cfg->policy != GSN_SERVE_OLDEST_FIRST && cfg->policy != GSN_SERVE_LEAST_WORK_FIRST))
+    return set_error(GSN_ERR_ARG, "bad server config");
   gsn_server* S = new gsn_server();
   S->cfg = *cfg;
   int rc = S->arena.init(cfg->hbm_budget_bytes);

@@ -14,7 +14,12 @@ from ._lib import check, load
 
 class ServerConfig(ctypes.Structure):
     _fields_ = [("hbm_budget_bytes", ctypes.c_uint64), ("max_inflight", ctypes.c_int32),
-                ("max_batch_jobs", ctypes.c_int32), ("max_launch_work", ctypes.c_uint64)]
+                ("max_batch_jobs", ctypes.c_int32), ("max_launch_work", ctypes.c_uint64),
+                ("policy", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+OLDEST_FIRST = 0       # GSN_SERVE_OLDEST_FIRST
+LEAST_WORK_FIRST = 1   # GSN_SERVE_LEAST_WORK_FIRST
 
 
 class Request(ctypes.Structure):
@@ -63,9 +68,9 @@ def _lib():
 
 class Server:
     def __init__(self, hbm_budget_bytes: int, max_inflight: int = 4, max_batch_jobs: int = 0,
-                 max_launch_work: int = 0):
+                 max_launch_work: int = 0, policy: int = OLDEST_FIRST):
         self.lib = _lib()
-        cfg = ServerConfig(hbm_budget_bytes, max_inflight, max_batch_jobs, max_launch_work)
+        cfg = ServerConfig(hbm_budget_bytes, max_inflight, max_batch_jobs, max_launch_work, policy, 0)
         h = ctypes.c_void_p()
         check(self.lib.gsn_server_create(ctypes.byref(cfg), ctypes.byref(h)))
         self.h = h
@@ -145,7 +150,7 @@ def poisson_trace(count: int, rate: float, seed: int, fields=(1, 2), lo=12, hi=2
 
 
 def bench_serving(g, torch, *, seconds: float = 1.0, rate: float = 2000.0, budget_gb: float = 120.0,
-                  max_inflight: int = 4, seed: int = 0x5EED0005) -> dict:
+                  max_inflight: int = 4, seed: int = 0x5EED0005, policy: int = OLDEST_FIRST) -> dict:
     """Config 5: Poisson stream at `rate` req/s for `seconds`, BLS12-381 / MNT4-753
     50/50, sizes 2^12..2^22, forward / inverse / coset-forward; 120 GB budget."""
     from . import BY_ID
@@ -162,7 +167,7 @@ def bench_serving(g, torch, *, seconds: float = 1.0, rate: float = 2000.0, budge
             a = np.ctypeslib.as_array(ctypes.cast(pin, ctypes.POINTER(ctypes.c_uint32)), shape=((1 << k) * f.limbs,))
             a[:] = f.device_random(1 << k, seed + 97 * k + fid).reshape(-1)
             bufs[(fid, k)] = (pin, pout)
-    srv = Server(int(budget_gb * (1 << 30)), max_inflight=max_inflight)
+    srv = Server(int(budget_gb * (1 << 30)), max_inflight=max_inflight, policy=policy)
     try:
         for fid in (1, 2):
             srv.warmup(fid, 12, 22)
@@ -191,4 +196,5 @@ def bench_serving(g, torch, *, seconds: float = 1.0, rate: float = 2000.0, budge
             "phase_ms_p99": {k: round(float(np.percentile(ph[:, i], 99)) * 1e3, 3) for i, k in enumerate(PHASES)},
             "p99_request_phases_ms": {k: round(float(ph[int(np.argsort(lat)[int(0.99 * (len(lat) - 1))]), i]) * 1e3, 3)
                                       for i, k in enumerate(PHASES)},
-            "budget_bytes": int(budget_gb * (1 << 30)), "max_inflight": max_inflight}
+            "budget_bytes": int(budget_gb * (1 << 30)), "max_inflight": max_inflight,
+            "policy": "least_work_first" if policy == LEAST_WORK_FIRST else "oldest_first"}

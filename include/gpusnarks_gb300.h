@@ -236,9 +236,19 @@ typedef struct gsn_server_config {
   int32_t max_batch_jobs;    /* cap on requests per launch (0 = 4096)             */
   uint64_t max_launch_work;  /* cap on the integer multiply-adds packed into one
                                 launch, (n/2) log2 n x 2(2s^2+s) per request;
-                                the oldest ready request always goes
+                                the leading ready request always goes
                                 (0 = 4e10, a few milliseconds of GPU time)       */
+  int32_t policy;            /* order in which ready requests are launched:
+                                GSN_SERVE_OLDEST_FIRST (0, default) or
+                                GSN_SERVE_LEAST_WORK_FIRST                       */
+  int32_t reserved;          /* 0                                                */
 } gsn_server_config;
+
+enum {
+  GSN_SERVE_OLDEST_FIRST = 0,    /* arrival order: bounded wait for every request     */
+  GSN_SERVE_LEAST_WORK_FIRST = 1 /* smallest transforms first: lower median latency
+                                    under overload, large requests wait longer     */
+};
 
 typedef struct gsn_request {
   int32_t field;

@@ -112,3 +112,12 @@ def test_entry_points_validate_before_touching_the_gpu(gsn):
         rc = call()
         assert rc == want and msg in lib.gsn_last_error(), (i, rc, lib.gsn_last_error())
     assert lib.gsn_ntt_host_batch(1, None, 0, 4, None, 0, None) == 0  # nothing to do
+
+
+def test_server_config_rejects_unknown_policy(gsn):
+    from gpusnarks_gb300.serve import ServerConfig
+    lib = gsn.load()
+    h = ctypes.c_void_p()
+    cfg = ServerConfig(1 << 30, 2, 0, 0, 7, 0)
+    assert lib.gsn_server_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
+    assert b"bad server config" in lib.gsn_last_error()

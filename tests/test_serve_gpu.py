@@ -143,3 +143,25 @@ def test_run_trace_empty(gsn, cuda_device):
         srv.close()
     assert lat.shape == (0,) and lat2.shape == (0,) and ph.shape == (0, 5)
     assert makespan == 0.0 and makespan2 == 0.0
+
+
+def test_least_work_first_policy_results_and_order(gsn, cuda_device):
+    """GSN_SERVE_LEAST_WORK_FIRST: every result equals the plain path, and under a backlog
+    the small requests finish before the large ones that arrived first."""
+    from gpusnarks_gb300.serve import LEAST_WORK_FIRST, Request, Server, TraceEntry
+    f = gsn.MNT4_753
+    sizes = [16, 16, 16, 16, 8, 8, 8, 8]  # large ones arrive first, all at once
+    ins = [f.random_array(1 << k, seed=4400 + i) for i, k in enumerate(sizes)]
+    outs = [np.empty_like(x) for x in ins]
+    want = [_plain(gsn, f, x, 0) for x in ins]
+    entries = [TraceEntry(0.0, Request(f.fid, k, 0, None, x.ctypes.data, o.ctypes.data))
+               for k, x, o in zip(sizes, ins, outs)]
+    srv = Server(1 << 30, max_inflight=1, max_launch_work=1, policy=LEAST_WORK_FIRST)
+    try:
+        srv.warmup(f.fid, 8, 16)
+        lat, _ = srv.run_trace(entries)
+    finally:
+        srv.close()
+    for o, w in zip(outs, want):
+        assert np.array_equal(o, w)
+    assert lat[4:].max() < lat[:4].max()
