@@ -181,7 +181,7 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
 }
 
 template <class P>
-__global__ void ntt_pass_kernel(PassArgs A) {
+__global__ void ntt_pass_kernel(const __grid_constant__ PassArgs A) {
   extern __shared__ uint4 gsn_smem[];
   uint32_t* sm = reinterpret_cast<uint32_t*>(gsn_smem);
   for (uint64_t t = blockIdx.x; t < A.tiles; t += gridDim.x) ntt_tile<P>(A, t, sm);

@@ -169,7 +169,7 @@ __device__ __forceinline__ uint32_t brev(uint32_t x, int bits) { return bits == 
 }  // namespace p32
 
 template <int ET, int LCG>
-__global__ void __launch_bounds__(512) ntt_p32_kernel(P32Args A) {
+__global__ void __launch_bounds__(512) ntt_p32_kernel(const __grid_constant__ P32Args A) {
   using namespace p32;
   extern __shared__ uint4 gsn_smem[];
   uint4* sm = gsn_smem;
@@ -404,7 +404,7 @@ __device__ __forceinline__ void store_fourstep(const P32Args& A, const uint4* sm
 // streams into the other buffer with cp.async.  The trailing __syncthreads of an iteration ends all reads
 // of the buffer the next iteration starts filling.  Same arithmetic and results as ntt_p32_fixed_kernel.
 template <int RL, int ET, int LCG>
-__global__ void __launch_bounds__(512) ntt_p32_pipe_kernel(P32Args A) {
+__global__ void __launch_bounds__(512) ntt_p32_pipe_kernel(const __grid_constant__ P32Args A) {
   using namespace p32;
   extern __shared__ uint4 gsn_smem[];
   constexpr uint32_t CG = 1u << LCG;
@@ -450,7 +450,7 @@ __global__ void __launch_bounds__(512) ntt_p32_pipe_kernel(P32Args A) {
 }
 
 template <int RL, int ET, int LCG>
-__global__ void __launch_bounds__(512) ntt_p32_fixed_kernel(P32Args A) {
+__global__ void __launch_bounds__(512) ntt_p32_fixed_kernel(const __grid_constant__ P32Args A) {
   using namespace p32;
   extern __shared__ uint4 gsn_smem[];
   uint4* sm = gsn_smem;
