@@ -1,10 +1,13 @@
 """Run one transform configuration a few times, for profilers.
 
     python -m gpusnarks_gb300.profile_case --field p32 --log-n 24 --reps 3
+    python -m gpusnarks_gb300.profile_case --field bls12_381_fr --batch 512 --batch-lo 10 --batch-hi 18
 
 Fills the input on the device (gsn_fill_random), runs `warmup` untimed and
-`reps` further transforms through the C ABI, prints the mean event time.  It
-is the command the committed ncu summaries under profiles/ were taken with.
+`reps` further transforms through the C ABI, prints the mean event time.
+With --batch J it runs J jobs of seeded log-uniform sizes 2^lo..2^hi as one
+persistent graph-captured launch (the batched path) instead.  It is the
+command the committed ncu summaries under profiles/ were taken with.
 """
 from __future__ import annotations
 
@@ -18,6 +21,9 @@ def main() -> None:
     ap.add_argument("--reps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=1)
     ap.add_argument("--direction", type=int, default=0)
+    ap.add_argument("--batch", type=int, default=0, help="jobs in one batched launch (0: one transform)")
+    ap.add_argument("--batch-lo", type=int, default=10)
+    ap.add_argument("--batch-hi", type=int, default=18)
     args = ap.parse_args()
 
     import torch
@@ -26,6 +32,9 @@ def main() -> None:
     from gpusnarks_gb300.batch import fill_random
 
     f = g.FIELDS[args.field]
+    if args.batch:
+        run_batch(g, torch, f, args)
+        return
     n = 1 << args.log_n
     data = torch.empty(n * f.limbs, dtype=torch.int32, device="cuda")
     fill_random(f, data, 0x5EED0000 + args.log_n)
@@ -40,6 +49,38 @@ def main() -> None:
     torch.cuda.synchronize()
     ms = s.elapsed_time(e) / max(args.reps, 1)
     print(f"{args.field} 2^{args.log_n}: {ms:.4f} ms per transform, {n / ms / 1e3:.1f} Melem/s")
+
+
+
+def run_batch(g, torch, f, args) -> None:
+    from gpusnarks_gb300.batch import Batch, fill_random, job_sizes
+
+    sizes = job_sizes(args.batch, args.batch_lo, args.batch_hi, 0x5EED0004)
+    total = sum(1 << k for k in sizes)
+    pool = torch.empty(total * f.limbs, dtype=torch.int32, device="cuda")
+    fill_random(f, pool, 0x5EED0004)
+    jobs, off = [], 0
+    for k in sizes:
+        jobs.append((pool.data_ptr() + off * f.limbs * 4, k, args.direction, None, None))
+        off += 1 << k
+    b = Batch(f, jobs, graph=True)
+    stream = torch.cuda.current_stream()
+    try:
+        for _ in range(args.warmup):
+            b.launch(stream)
+        torch.cuda.synchronize()
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record()
+        for _ in range(args.reps):
+            b.launch(stream)
+        e.record()
+        torch.cuda.synchronize()
+        b.status()
+    finally:
+        b.close()
+    ms = s.elapsed_time(e) / max(args.reps, 1)
+    print(f"{args.field} batch of {args.batch} (2^{args.batch_lo}..2^{args.batch_hi}, {total} elements): "
+          f"{ms:.4f} ms per launch, {total / ms / 1e3:.1f} Melem/s")
 
 
 if __name__ == "__main__":
