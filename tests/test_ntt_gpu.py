@@ -41,6 +41,21 @@ def test_forward_matches_oracle(gsn, cuda_device, fname, log_n):
     assert np.array_equal(got, want)
 
 
+@pytest.mark.parametrize("fname,max_log", [("p32", 22), ("bls12_381_fr", 20), ("mnt4753_fr", 19)])
+def test_every_size_matches_oracle(gsn, cuda_device, fname, max_log):
+    """Every size from 2^0 up, so every plan of the tuned table in that range runs: forward against the
+    oracle, then the inverse back to the input."""
+    f = gsn.FIELDS[fname]
+    for log_n in range(max_log + 1):
+        x = f.random_array(1 << log_n, seed=SEED + 1000 + 31 * log_n + f.fid)
+        d = gsn.to_device(x)
+        gsn.ntt(f, d)
+        got = gsn.to_host(d).reshape(x.shape)
+        assert np.array_equal(got, O.ntt(f.fid, x).reshape(x.shape)), log_n
+        gsn.ntt(f, d, direction=gsn.INVERSE)
+        assert np.array_equal(gsn.to_host(d).reshape(x.shape), x), log_n
+
+
 def test_config1_p32_n65536(gsn, cuda_device):
     """p = 3*2^30+1, n = 2^16, seeded uniform inputs, omega = 5^((p-1)/n)."""
     f = gsn.P32
