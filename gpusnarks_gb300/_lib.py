@@ -74,6 +74,7 @@ _SIGNATURES = [
                                       ctypes.POINTER(ctypes.c_uint64), ctypes.POINTER(ctypes.c_uint64),
                                       ctypes.POINTER(ctypes.c_uint64)]),
     ("gsn_batch_destroy", ctypes.c_int, [ctypes.c_void_p]),
+    ("gsn_ntt_batch", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]),
     ("gsn_batch_selftest_wait", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_uint32)]),
     ("gsn_fill_random", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_uint64,
                                        ctypes.c_void_p]),

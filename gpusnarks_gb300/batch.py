@@ -12,25 +12,43 @@ import numpy as np
 from ._lib import BatchJob, check, load
 
 
+def _job_array(field, jobs):
+    """(ctypes gsn_batch_job array, arrays it points into) for jobs of
+    (device_ptr:int, log_n:int, direction:int, omega, shift)."""
+    from . import _limbs  # late import: package init order
+
+    keep = []
+    arr = (BatchJob * len(jobs))()
+    for i, (ptr, log_n, direction, omega, shift) in enumerate(jobs):
+        w = _limbs(field, omega)
+        s = _limbs(field, shift)
+        keep += [w, s]
+        arr[i].data = ptr
+        arr[i].log_n = log_n
+        arr[i].dir = direction
+        arr[i].omega = None if w is None else w.ctypes.data
+        arr[i].shift = None if s is None else s.ctypes.data
+    return arr, keep
+
+
+def ntt_batch(field, jobs, *, stream=None) -> None:
+    """gsn_ntt_batch: transform every job in one persistent launch and wait for it."""
+    from . import _stream_handle, field_of
+
+    f = field_of(field)
+    arr, _keep = _job_array(f, jobs)
+    check(load().gsn_ntt_batch(f.fid, ctypes.cast(arr, ctypes.c_void_p), len(jobs), _stream_handle(stream)))
+
+
 class Batch:
     GRAPH = 1
 
     def __init__(self, field, jobs, *, graph: bool = True):
         """jobs: iterable of (device_ptr:int, log_n:int, direction:int, omega, shift)."""
-        from . import _limbs, field_of  # late import: package init order
+        from . import field_of  # late import: package init order
 
         self.field = field_of(field)
-        self._keep = []
-        arr = (BatchJob * len(jobs))()
-        for i, (ptr, log_n, direction, omega, shift) in enumerate(jobs):
-            w = _limbs(self.field, omega)
-            s = _limbs(self.field, shift)
-            self._keep += [w, s]
-            arr[i].data = ptr
-            arr[i].log_n = log_n
-            arr[i].dir = direction
-            arr[i].omega = None if w is None else w.ctypes.data
-            arr[i].shift = None if s is None else s.ctypes.data
+        arr, self._keep = _job_array(self.field, jobs)
         self._jobs = arr
         h = ctypes.c_void_p()
         check(load().gsn_batch_create(self.field.fid, ctypes.cast(arr, ctypes.c_void_p), len(jobs),

@@ -274,6 +274,19 @@ int gsn_batch_destroy(gsn_batch* b) {
   return GSN_OK;
 }
 
+int gsn_ntt_batch(int field, const gsn_batch_job* jobs, size_t njobs, void* stream) {
+  gsn_batch* b = nullptr;
+  int rc = gsn_batch_create(field, jobs, njobs, 0, &b);
+  if (rc) return rc;
+  rc = gsn_batch_launch(b, stream);
+  if (!rc) {
+    cudaError_t e = cudaStreamSynchronize(static_cast<cudaStream_t>(stream));
+    rc = e != cudaSuccess ? cuda_fail(e, "batch wait") : gsn_batch_status(b);
+  }
+  const int drc = gsn_batch_destroy(b);
+  return rc ? rc : drc;
+}
+
 int gsn_batch_selftest_wait(int field, int drop_first_pass, uint32_t* status_out) {
   const FieldOps* F = field_ops(field);
   if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);

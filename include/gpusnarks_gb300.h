@@ -197,6 +197,11 @@ int gsn_batch_status(gsn_batch* b);
 /* njobs, work items (tiles), total elements, device bytes held */
 int gsn_batch_info(gsn_batch* b, uint64_t* njobs, uint64_t* nwork, uint64_t* elements, uint64_t* device_bytes);
 int gsn_batch_destroy(gsn_batch* b);
+/* One-shot: gsn_batch_create + one persistent launch on `stream` + wait for
+ * that stream + gsn_batch_status + gsn_batch_destroy.  Returns when every job
+ * is transformed.  For repeated batches of the same shapes keep a gsn_batch
+ * (its plan, scratch and graph are built once). */
+int gsn_ntt_batch(int field, const gsn_batch_job* jobs, size_t njobs, void* stream);
 /* Self-test of the batch kernel's bounded dependency wait: one 2^12 job with
  * a ~1 ms wait limit.  drop_first_pass = 1 leaves its first pass out of the
  * work queue, so every later tile's wait must expire: *status_out becomes

@@ -112,3 +112,30 @@ def test_batch_rejects_empty_job_list(gsn, cuda_device):
     from gpusnarks_gb300.batch import Batch
     with pytest.raises(gsn.GsnError, match="ARG"):
         Batch(gsn.BLS12_381, [])
+
+
+def test_one_shot_ntt_batch(gsn, cuda_device):
+    """gsn_ntt_batch equals a kept Batch's launch and returns with the work done."""
+    import torch
+    from gpusnarks_gb300.batch import Batch, ntt_batch
+    f = gsn.MNT4_753
+    sizes = [9, 3, 12, 0, 1, 10, 6]
+    dirs = [0, 1, 2, 0, 1, 2, 0]
+    xs = [f.random_array(1 << k, seed=7300 + i) for i, k in enumerate(sizes)]
+    a = [gsn.to_device(x) for x in xs]
+    b = [gsn.to_device(x) for x in xs]
+    ntt_batch(f, [(t.data_ptr(), k, d, None, None) for t, k, d in zip(a, sizes, dirs)])
+    kept = Batch(f, [(t.data_ptr(), k, d, None, None) for t, k, d in zip(b, sizes, dirs)], graph=False)
+    try:
+        kept.launch()
+        torch.cuda.synchronize()
+        kept.status()
+    finally:
+        kept.close()
+    for ta, tb in zip(a, b):
+        assert torch.equal(ta, tb)
+    for x, t, k, d in zip(xs, a, sizes, dirs):
+        if d == 0:
+            assert np.array_equal(gsn.to_host(t).reshape(x.shape), O.ntt(f.fid, x).reshape(x.shape))
+    with pytest.raises(gsn.GsnError, match="ARG"):
+        ntt_batch(f, [])

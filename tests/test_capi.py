@@ -101,6 +101,7 @@ def test_entry_points_validate_before_touching_the_gpu(gsn):
         (lambda: lib.gsn_qap_h(1, fake, fake, ctypes.c_void_p(0x20000), 4, None, None), ARG, b"distinct"),
         (lambda: lib.gsn_fft_ref_compat(fake, 30, wp, 3, None), SIZE, b"2^24"),
         (lambda: lib.gsn_batch_create(1, None, 3, 0, None), ARG, b"null"),
+        (lambda: lib.gsn_ntt_batch(1, None, 0, None), ARG, b"empty batch"),
         (lambda: lib.gsn_server_create(None, None), ARG, b"null"),
         (lambda: lib.gsn_server_submit(None, None, None), ARG, b"null"),
         (lambda: lib.gsn_fill_random(1, None, 16, 1, None), ARG, b"null"),
