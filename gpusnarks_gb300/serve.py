@@ -151,7 +151,7 @@ def poisson_trace(count: int, rate: float, seed: int, fields=(1, 2), lo=12, hi=2
 
 def bench_serving(g, torch, *, seconds: float = 1.0, rate: float = 2000.0, budget_gb: float = 120.0,
                   max_inflight: int = 4, seed: int = 0x5EED0005, policy: int = OLDEST_FIRST) -> dict:
-    """Config 5: Poisson stream at `rate` req/s for `seconds`, BLS12-381 / MNT4-753
+    """The mixed serving stream: Poisson arrivals at `rate` req/s for `seconds`, BLS12-381 / MNT4-753
     50/50, sizes 2^12..2^22, forward / inverse / coset-forward; 120 GB budget."""
     from . import BY_ID
     trace = poisson_trace(max(1, int(rate * seconds)), rate, seed)
