@@ -601,11 +601,9 @@ extern "C" int gsn_microbench_imad(int iters, double* mads_per_s, double* mads_p
   *mads_per_s = mads / (ms * 1e-3);
   // clock: cycles / ns of each block, median over blocks
   std::vector<double> mhz;
-  double cyc_sum = 0;
   for (int b = 0; b < grid; ++b) {
     const double ns = (double)(ht[2 * b + 1] - ht[2 * b]);
     if (ns > 0) mhz.push_back((double)hc[b] / ns * 1e3);
-    cyc_sum += (double)hc[b];
   }
   double med = 0;
   if (!mhz.empty()) {
@@ -613,9 +611,9 @@ extern "C" int gsn_microbench_imad(int iters, double* mads_per_s, double* mads_p
     med = mhz[mhz.size() / 2];
   }
   if (sm_mhz) *sm_mhz = med;
-  // mads per SM per cycle: blocks on one SM run concurrently, so an SM's busy
-  // cycles are about the mean block duration.
-  const double cyc_per_block = cyc_sum / grid;
-  if (mads_per_clk_sm) *mads_per_clk_sm = mads / sms / cyc_per_block;
+  // mads per SM per cycle over the whole launch (event time x the measured clock).  Not over a block's own
+  // span: blocks resident on one SM together do not progress equally, so the mean block is shorter than the
+  // SM's busy time.
+  if (mads_per_clk_sm) *mads_per_clk_sm = med > 0 ? mads / sms / (ms * 1e-3 * med * 1e6) : 0.0;
   return GSN_OK;
 }
