@@ -165,3 +165,41 @@ def test_least_work_first_policy_results_and_order(gsn, cuda_device):
     for o, w in zip(outs, want):
         assert np.array_equal(o, w)
     assert lat[4:].max() < lat[:4].max()
+
+
+def test_request_lifecycle_errors(gsn, cuda_device):
+    """Every misuse of a request id comes back as its own error, and the server stays usable."""
+    import ctypes
+
+    from gpusnarks_gb300.serve import Request, Server
+    f = gsn.BLS12_381
+    x = f.random_array(1 << 10, seed=4500)
+    want = _plain(gsn, f, x, 0)
+    srv = Server(1 << 28, max_inflight=2)
+    try:
+        with pytest.raises(gsn.GsnError, match="ARG"):
+            srv.wait(987654321)
+        with pytest.raises(gsn.GsnError, match="ARG"):
+            srv.release(987654321)
+        with pytest.raises(gsn.GsnError, match="ARG"):
+            srv.submit(f, x, 7)  # no such direction
+        rid_c = ctypes.c_uint64()
+        too_big = Request(f.fid, 40, 0, None, x.ctypes.data, None)
+        assert srv.lib.gsn_server_submit(srv.h, ctypes.byref(too_big), ctypes.byref(rid_c)) == 3  # SIZE
+        assert srv.lib.gsn_server_submit(srv.h, None, ctypes.byref(rid_c)) == 1  # ARG
+        out = np.empty_like(x)
+        rid = srv.submit(f, x, 0, host_out=out)  # result copied out: nothing stays resident
+        srv.wait(rid)
+        with pytest.raises(gsn.GsnError, match="STATE"):
+            srv.fetch(rid, np.empty_like(x))
+        srv.release(rid)
+        with pytest.raises(gsn.GsnError, match="ARG"):
+            srv.release(rid)  # already released
+        assert np.array_equal(out, want)
+        rid = srv.submit(f, x, 0)  # resident result
+        srv.wait(rid)
+        got = srv.fetch(rid, np.empty_like(x))
+        srv.release(rid)
+        assert np.array_equal(got, want)
+    finally:
+        srv.close()
