@@ -3,7 +3,13 @@
 Every CUDA translation unit under csrc/ is compiled for sm_103a only
 (``-gencode arch=compute_103a,code=sm_103a``) by nvcc, in parallel, into
 gpusnarks_gb300/_build/, then linked into gpusnarks_gb300/_lib/.  Objects
-are rebuilt when their source or any header in csrc/ or include/ is newer.
+are rebuilt when their source or any header in csrc/ or include/ is newer,
+or when the build-time options below change.
+
+Build-time options (environment variables, passed to nvcc as -D defines):
+  GSN_MONT_SCHEDULE  Montgomery product schedule of the multi-limb fields:
+                     1 even/odd accumulators (default), 0 row chains,
+                     2 split accumulators with a carried merge.
 """
 from __future__ import annotations
 
@@ -43,8 +49,22 @@ def _headers_mtime() -> float:
     return max((h.stat().st_mtime for h in hs), default=0.0)
 
 
+OPTIONS = ("GSN_MONT_SCHEDULE",)
+
+
+def _defines() -> list[str]:
+    out = []
+    for name in OPTIONS:
+        v = os.environ.get(name)
+        if v:
+            if not v.isdigit():
+                raise ValueError(f"{name} must be a number, got {v!r}")
+            out.append(f"-D{name}={v}")
+    return out
+
+
 def _compile(src: pathlib.Path, obj: pathlib.Path, verbose: bool) -> str:
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *_defines(), "-c", str(src), "-o", str(obj)]
     if src.suffix == ".cpp":
         cmd[1:1] = ["-x", "cu"]
     if verbose:
@@ -58,6 +78,10 @@ def _compile(src: pathlib.Path, obj: pathlib.Path, verbose: bool) -> str:
 def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -> pathlib.Path:
     BUILD.mkdir(exist_ok=True)
     LIBDIR.mkdir(exist_ok=True)
+    stamp = BUILD / "options.txt"
+    opts = " ".join(_defines())
+    if not stamp.exists() or stamp.read_text() != opts:
+        force = True
     hdr_t = _headers_mtime()
     todo = []
     objs = []
@@ -81,6 +105,7 @@ def build(force: bool = False, verbose: bool = False, jobs: int | None = None) -
         if res.returncode != 0:
             raise RuntimeError(f"link failed:\n{res.stdout}\n{res.stderr}")
         os.replace(tmp, LIB)
+    stamp.write_text(opts)
     return LIB
 
 
