@@ -16,6 +16,7 @@
 #include <cstring>
 #include <fstream>
 #include <map>
+#include <mutex>
 #include <sstream>
 #include <string>
 #include <vector>
@@ -181,7 +182,8 @@ std::string plan_json(int field, const Plan& p, float ms, int mode) {
   return o.str();
 }
 
-std::map<std::tuple<int, int, int>, float> g_tuned_ms;  // (field, log_n, mode)
+std::mutex g_tuned_ms_mu;
+std::map<std::tuple<int, int, int>, float> g_tuned_ms;  // (field, log_n, mode), under g_tuned_ms_mu
 
 // Minimal reader for the files plan_json writes: finds "key": value or
 // "key": [a, b, c, d] inside one object.
@@ -250,7 +252,10 @@ static int autotune_impl(int field, uint32_t lo, uint32_t hi, int reps, int mode
                    timed, skipped, best_ms);
     if (best_ms < 1e30f) {
       set_tuned_plan(F->id, (int)k, best, mode);
-      g_tuned_ms[std::make_tuple(F->id, (int)k, mode)] = best_ms;
+      {
+        std::lock_guard<std::mutex> g(g_tuned_ms_mu);
+        g_tuned_ms[std::make_tuple(F->id, (int)k, mode)] = best_ms;
+      }
     }
   }
   cudaDeviceSynchronize();
@@ -281,9 +286,13 @@ int gsn_tuning_save(const char* path) {
       for (int k = 0; k <= F->max_log_n; ++k) {
         Plan p;
         if (!get_tuned_plan(field, k, &p, mode)) continue;
-        auto it = g_tuned_ms.find(std::make_tuple(field, k, mode));
-        f << (first ? "" : ",\n") << "    "
-          << plan_json(field, p, it == g_tuned_ms.end() ? -1.0f : it->second, mode);
+        float ms = -1.0f;
+        {
+          std::lock_guard<std::mutex> g(g_tuned_ms_mu);
+          auto it = g_tuned_ms.find(std::make_tuple(field, k, mode));
+          if (it != g_tuned_ms.end()) ms = it->second;
+        }
+        f << (first ? "" : ",\n") << "    " << plan_json(field, p, ms, mode);
         first = false;
       }
     }
@@ -327,6 +336,7 @@ int gsn_tuning_load(const char* path) {
 
 int gsn_tuning_clear(void) {
   clear_tuned_plans();
+  std::lock_guard<std::mutex> g(g_tuned_ms_mu);
   g_tuned_ms.clear();
   return GSN_OK;
 }
