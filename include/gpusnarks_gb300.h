@@ -6,6 +6,15 @@
  * gsn_last_error() gives the message of the last failure on the calling
  * thread.  No function takes or returns a torch or C++ type.
  *
+ * Threading: any host thread may call any entry point.  Transforms issued on
+ * different streams run concurrently: each stream gets its own library
+ * scratch, and the twiddle-table cache is locked.  Exceptions:
+ *   - a gsn_batch handle is used by one thread at a time;
+ *   - a gsn_server's submit / wait / fetch / release / stats may come from any
+ *     thread, but gsn_server_destroy only when no other call on it is running;
+ *   - gsn_ntt_noalloc calls share one scratch array and must not overlap;
+ *   - gsn_release_caches must not run while other calls are in flight.
+ *
  * Element layout (all fields): an element is LIMBS little-endian uint32
  * words, exactly the reference's `uint32_t im_rep[SIZE]`
  * (cuda/device_field.h:75); an array of n elements is n*LIMBS words,
