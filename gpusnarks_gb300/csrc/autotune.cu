@@ -193,6 +193,12 @@ bool find_int(const std::string& obj, const char* key, int* v) {
   if (p == std::string::npos) return false;
   return std::sscanf(obj.c_str() + p + k.size(), " %d", v) == 1;
 }
+bool find_float(const std::string& obj, const char* key, float* v) {
+  const std::string k = std::string("\"") + key + "\":";
+  size_t p = obj.find(k);
+  if (p == std::string::npos) return false;
+  return std::sscanf(obj.c_str() + p + k.size(), " %f", v) == 1;
+}
 bool find_arr(const std::string& obj, const char* key, int* v) {
   const std::string k = std::string("\"") + key + "\":";
   size_t p = obj.find(k);
@@ -329,6 +335,11 @@ int gsn_tuning_load(const char* path) {
     const FieldOps* F = field_ops(field);
     if (!F || !plan_valid(*F, p) || mode < 0 || mode > 1) continue;
     set_tuned_plan(field, p.log_n, p, mode);
+    float ms = -1.0f;  // the measured time travels with the plan, so a save of a loaded table keeps it
+    if (find_float(obj, "ms", &ms) && ms >= 0) {
+      std::lock_guard<std::mutex> g(g_tuned_ms_mu);
+      g_tuned_ms[std::make_tuple(field, p.log_n, mode)] = ms;
+    }
     ++loaded;
   }
   return loaded > 0 ? GSN_OK : set_error(GSN_ERR_ARG, "no valid plans in %s", path);

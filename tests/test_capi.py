@@ -122,3 +122,31 @@ def test_server_config_rejects_unknown_policy(gsn):
     cfg = ServerConfig(1 << 30, 2, 0, 0, 7, 0)
     assert lib.gsn_server_create(ctypes.byref(cfg), ctypes.byref(h)) == 1
     assert b"bad server config" in lib.gsn_last_error()
+
+
+def test_tuning_table_save_load_round_trip(gsn, tmp_path):
+    """The committed table loads without a GPU, and saving then reloading it keeps every plan and time."""
+    import json
+    lib = gsn.load()
+    table = ROOT / "gpusnarks_gb300" / "tuning" / "gb300.json"
+    assert lib.gsn_tuning_load(str(table).encode()) == 0
+    buf = ctypes.create_string_buffer(512)
+
+    def describe(fid, k):
+        assert lib.gsn_plan_describe(fid, k, buf, 512) == 0
+        d = json.loads(buf.value)
+        d.pop("ms", None)
+        return d
+
+    before = {(fid, k): describe(fid, k) for fid in (0, 1, 2) for k in range(8, 21)}
+    out = tmp_path / "saved.json"
+    assert lib.gsn_tuning_save(str(out).encode()) == 0
+    saved = json.loads(out.read_text())["plans"]
+    orig = json.loads(table.read_text())["plans"]
+    key = lambda p: (p["field"], p["mode"], p["log_n"])
+    assert sorted(map(key, saved)) == sorted(map(key, orig))
+    assert {key(p): p["ms"] for p in saved} == pytest.approx({key(p): p["ms"] for p in orig}, rel=1e-4)
+    assert lib.gsn_tuning_clear() == 0
+    assert lib.gsn_tuning_load(str(out).encode()) == 0
+    assert {(fid, k): describe(fid, k) for fid in (0, 1, 2) for k in range(8, 21)} == before
+    assert lib.gsn_tuning_load(str(table).encode()) == 0
