@@ -136,11 +136,15 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
         }
         mul = true;
       } else if (stage) {
+        // Butterfly b = (i, group, jj) with the twiddle index i slowest: the 2^(lr-1-log_half) * J
+        // butterflies of twiddle 1 (i = 0) are then consecutive threads, so in the late stages whole warps
+        // skip the product instead of idling beside lanes that compute it.
         const int log_half = lr - 1 - ph;
+        const int groups_log = ph;  // (lr - 1) - log_half
         const int jj = b & (J - 1);
-        const int bb = b >> lj;
-        const int i = bb & ((1 << log_half) - 1);
-        const int u = ((bb >> log_half) << (log_half + 1)) + i;
+        const int group = (b >> lj) & ((1 << groups_log) - 1);
+        const int i = b >> (groups_log + lj);
+        const int u = (group << (log_half + 1)) + i;
         const int v = u + (1 << log_half);
         Fe<P> y, sum;
         fe_load<P>(x, sm + ((u << lj) + jj) * N);
