@@ -70,3 +70,80 @@ def test_concurrent_host_calls(gsn, cuda_device):
     assert not errors, errors
     for a, w in zip(work, want):
         assert np.array_equal(a, w)
+
+
+def test_server_clients_on_several_threads(gsn, cuda_device):
+    """Four client threads submit to one server and wait on their own requests at the same time."""
+    from gpusnarks_gb300.serve import Server
+    rng = np.random.default_rng(SEED + 77)
+    reqs = []
+    for i in range(32):
+        f = (gsn.BLS12_381, gsn.MNT4_753)[int(rng.integers(0, 2))]
+        k = int(rng.integers(6, 13))
+        d = int(rng.integers(0, 3))
+        reqs.append((f, k, d, f.random_array(1 << k, seed=SEED + 500 + i)))
+    want = []
+    for f, k, d, x in reqs:
+        t = gsn.to_device(x)
+        gsn.ntt(f, t, direction=d)
+        want.append(gsn.to_host(t).reshape(x.shape))
+    got = [None] * len(reqs)
+    errors = []
+    srv = Server(1 << 30, max_inflight=3)
+
+    def client(t):
+        try:
+            for i in range(t, len(reqs), 4):
+                f, k, d, x = reqs[i]
+                out = np.empty_like(x)
+                rid = srv.submit(f, x, d, host_out=out)
+                srv.wait(rid)
+                srv.release(rid)
+                got[i] = out
+        except Exception as exc:  # reported below
+            errors.append(exc)
+
+    try:
+        threads = [threading.Thread(target=client, args=(t,)) for t in range(4)]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join(120)
+    finally:
+        srv.close()
+    assert not errors, errors
+    for g_, w in zip(got, want):
+        assert np.array_equal(g_, w)
+
+
+def test_one_shot_batches_on_several_threads(gsn, cuda_device):
+    """gsn_ntt_batch from four threads, each on its own stream, at the same time."""
+    import torch
+    from gpusnarks_gb300.batch import ntt_batch
+    f = gsn.BLS12_381
+    sizes = [[10, 4, 8], [12, 6], [9, 9, 9, 3], [11, 0, 7]]
+    xs = [[f.random_array(1 << k, seed=SEED + 900 + 10 * t + j) for j, k in enumerate(ks)]
+          for t, ks in enumerate(sizes)]
+    want = [[O.ntt(f.fid, x).reshape(x.shape) for x in row] for row in xs]
+    got = [None] * len(sizes)
+    errors = []
+
+    def worker(t):
+        try:
+            s = torch.cuda.Stream()
+            ds = [gsn.to_device(x) for x in xs[t]]
+            torch.cuda.current_stream().synchronize()
+            ntt_batch(f, [(d.data_ptr(), k, 0, None, None) for d, k in zip(ds, sizes[t])], stream=s)
+            got[t] = [gsn.to_host(d).reshape(x.shape) for d, x in zip(ds, xs[t])]
+        except Exception as exc:  # reported below
+            errors.append(exc)
+
+    threads = [threading.Thread(target=worker, args=(t,)) for t in range(4)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join(120)
+    assert not errors, errors
+    for grow, wrow in zip(got, want):
+        for g_, w in zip(grow, wrow):
+            assert np.array_equal(g_, w)
