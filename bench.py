@@ -55,6 +55,14 @@ REF_Q = int("4189849096791895340234421479124063712817070991995394907178350292102
 
 
 # --------------------------------------------------------------------------- utils
+def headline_config(ws: int) -> dict:
+    """The workload's `config`, printed identically by both arms."""
+    return {"workload": "forward NTT, MNT4-753 scalar field r (24 limbs), n=2^18, per GPU",
+            "field": "mnt4753_fr", "log_n": HEADLINE_LOG_N, "elements_per_step": 1 << HEADLINE_LOG_N,
+            "l2": "GPU arm: flushed (256 MB write) before each step; input 25 MB < L2",
+            "parallelism": f"replicas x{ws}"}
+
+
 def dist_init():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -364,7 +372,115 @@ def p32_sweep(g, torch, flush, hbm_gbs, steps=5):
                              "hbm_frac": round(B / t / 1e9 / hbm_gbs, 4),
                              "single_pass_frac": round(8 * n / t / 1e9 / hbm_gbs, 4), "p_min": pmin}
     out["2^26"]["dram_bytes_per_launch"] = profiled_traffic("ntt_p32_fixed_kernel 2^26")
+    # the CPU restatement beside the sizes it finishes in seconds (the reference's README times its CPU FFT
+    # at 2^20 and 2^22 only and reports 2^25 and 2^28 as not finished)
+    for log_n in (20, 22):
+        out[f"2^{log_n}"]["cpu_port"] = cpu_port_rate(0, log_n, g.P32.device_random(1 << log_n, SEED + log_n))
     return out
+
+
+def cpu_threads() -> tuple[int, int]:
+    """(threads, log_cpus) for the CPU restatement: every host core, num_cpus = the largest power of two."""
+    threads = os.cpu_count() or 1
+    return threads, max(0, int(math.floor(math.log2(threads))))
+
+
+def cpu_port_rate(fid: int, log_n: int, x, reps: int = 1) -> dict:
+    """The oracle's restatement of the reference host FFT (fixed butterfly) on all host cores: median of
+    `reps` full transforms of `x` (one untimed first)."""
+    import oracle
+    threads, log_cpus = cpu_threads()
+    w = oracle.root(fid, log_n)
+    oracle.fft(fid, x, w, log_cpus=log_cpus, nthreads=threads)
+    ts = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        oracle.fft(fid, x, w, log_cpus=log_cpus, nthreads=threads)
+        ts.append(time.perf_counter() - t0)
+    t = float(np.median(ts))
+    return {"ms": round(t * 1e3, 3), "Melem_s": round((1 << log_n) / t / 1e6, 4), "cores": threads,
+            "log_cpus": log_cpus, "kind": "port"}
+
+
+def config1_p32_2_16(g, torch, flush, hbm_gbs, steps=20):
+    """Plain forward NTT over p32 at n = 2^16 (the reference's README row 'FFT 32-bit n=2^16'):
+    device-resident time (L2 flushed before each step) against the HBM roofline with P_min = 1, the
+    whole best_fft-style call from host memory (gsn_ntt_host), the output checked against the oracle, and
+    the CPU restatement beside it."""
+    import oracle
+    f = g.P32
+    log_n = 16
+    n = 1 << log_n
+    ts, _ = time_device_ntt(g, torch, f, log_n, steps, 3, flush=flush)
+    t = float(np.median(ts))
+    x = f.device_random(n, SEED + log_n)
+    d = g.to_device(x)
+    g.ntt(f, d)
+    verified = bool(np.array_equal(g.to_host(d), oracle.ntt(0, x)))
+    e2e, _ = time_e2e_host(g, f, log_n, steps, 3)
+    te = float(np.median(e2e))
+    B = 2 * 4 * n
+    return {"ms": round(t * 1e3, 4), "Melem_s": round(n / t / 1e6, 1), "hbm_frac": round(B / t / 1e9 / hbm_gbs, 4),
+            "p_min": 1, "host_call_ms": round(te * 1e3, 4), "host_call_Melem_s": round(n / te / 1e6, 1),
+            "host_call_api": "gsn_ntt_host on pinned memory (copy in, transform, copy out)",
+            "verified_vs_oracle": verified, "cpu_port": cpu_port_rate(0, log_n, x, reps=5),
+            "published_reference_s": {"gpu": 0.32, "cpu": 0.21, "where": "README.md:30, GTX 1080 / Xeon"}}
+
+
+def poly_product_2_21(g, torch, reps=5):
+    """Config 3's companion: two seeded polynomials with 2^20 coefficients multiplied by forward NTTs of
+    size 2^21, a pointwise product and an inverse NTT, device-resident (inputs > L2 in total: 2 x 8 MiB is
+    not, so L2 is not flushed: this times the four launches back to back as a prover would run them).
+    Checked against the oracle's NTT product; the CPU restatement of the same three transforms beside it."""
+    import oracle
+    f = g.P32
+    P = f.p
+    m = 1 << 20
+    a = f.device_random(m, SEED + 3 * 100 + 1)
+    b = f.device_random(m, SEED + 3 * 100 + 2)
+    A = np.zeros(2 * m, dtype=np.uint32)
+    B = np.zeros(2 * m, dtype=np.uint32)
+    A[:m], B[:m] = a, b
+    dA0, dB0 = g.to_device(A), g.to_device(B)
+    dA, dB = dA0.clone(), dB0.clone()
+    stream = torch.cuda.current_stream()
+
+    def run():
+        g.ntt(f, dA)
+        g.ntt(f, dB)
+        g.pointwise_mul(f, dA, dB)
+        g.ntt(f, dA, direction=g.INVERSE)
+
+    run()
+    torch.cuda.synchronize()
+    c = g.to_host(dA)
+    ts = []
+    for _ in range(reps):
+        dA.copy_(dA0)
+        dB.copy_(dB0)
+        s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        s.record(stream)
+        run()
+        e.record(stream)
+        e.synchronize()
+        ts.append(s.elapsed_time(e) * 1e-3)
+    t = float(np.median(ts))
+    # CPU: the restated host FFT for the three transforms, numpy for the pointwise product and n^-1
+    threads, log_cpus = cpu_threads()
+    w = oracle.root(0, 21)
+    t0 = time.perf_counter()
+    Ao = oracle.fft(0, A, w, log_cpus=log_cpus, nthreads=threads)
+    Bo = oracle.fft(0, B, w, log_cpus=log_cpus, nthreads=threads)
+    prod = ((Ao.astype(np.uint64) * Bo.astype(np.uint64)) % np.uint64(P)).astype(np.uint32)
+    y = oracle.fft(0, prod, pow(w, P - 2, P), log_cpus=log_cpus, nthreads=threads)
+    want = ((y.astype(np.uint64) * np.uint64(pow(2 * m, P - 2, P))) % np.uint64(P)).astype(np.uint32)
+    t_cpu = time.perf_counter() - t0
+    return {"ms": round(t * 1e3, 4), "transforms": 3, "pointwise": 1,
+            "Melem_s": round(3 * 2 * m / t / 1e6, 1),
+            "coefficients_per_s_M": round(2 * m / t / 1e6, 1),
+            "verified_vs_oracle": bool(np.array_equal(c, want)),
+            "cpu_port": {"ms": round(t_cpu * 1e3, 1), "cores": threads, "log_cpus": log_cpus, "kind": "port",
+                         "what": "three restated host FFTs of 2^21 + numpy pointwise product and n^-1 scale"}}
 
 
 def batch_vs_per_call(g, torch, njobs=4096, lo=10, hi=20, reps=3):
@@ -380,6 +496,19 @@ def batch_vs_per_call(g, torch, njobs=4096, lo=10, hi=20, reps=3):
         off += 1 << k
     b = Batch(f, jobs, graph=True)
     stream = torch.cuda.current_stream()
+    # a seeded sample of jobs is checked after the first batched launch against the plain per-call path
+    # (gsn_ntt on a copy of the same input); every size class 2^lo..2^hi is in the sample
+    rng = np.random.default_rng(SEED + 44)
+    by_size: dict[int, list[int]] = {}
+    for i, k in enumerate(sizes):
+        by_size.setdefault(k, []).append(i)
+    sample = sorted({int(rng.choice(v)) for v in by_size.values()} |
+                    {int(i) for i in rng.choice(njobs, size=min(njobs, 32), replace=False)})
+    offs = np.cumsum([0] + [1 << k for k in sizes])
+    views = {i: pool[int(offs[i]) * f.limbs:int(offs[i + 1]) * f.limbs] for i in sample}
+    want = {i: v.clone() for i, v in views.items()}
+    for i, w in want.items():
+        g.ntt(f, w)
 
     def timed(fn):
         ts = []
@@ -394,6 +523,9 @@ def batch_vs_per_call(g, torch, njobs=4096, lo=10, hi=20, reps=3):
         return float(np.median(ts))
 
     b.launch()
+    torch.cuda.synchronize()
+    b.status()
+    verified = all(torch.equal(views[i], want[i]) for i in sample)
     b.launch_per_call()
     torch.cuda.synchronize()
     t_batch = timed(lambda: b.launch())
@@ -404,7 +536,23 @@ def batch_vs_per_call(g, torch, njobs=4096, lo=10, hi=20, reps=3):
     del pool
     torch.cuda.empty_cache()
     work = sum(imad_work(f, k) for k in sizes)
+    # CPU restatement on a bounded subset: the sampled jobs up to 2^16 (every size class up to there)
+    import oracle
+    threads, log_cpus = cpu_threads()
+    cpu_jobs = [i for i in sample if sizes[i] <= 16]
+    cpu_el, t0 = 0, time.perf_counter()
+    for i in cpu_jobs:
+        x = f.device_random(1 << sizes[i], SEED + 4400 + i)
+        oracle.fft(1, x, oracle.root(1, sizes[i]), log_cpus=min(log_cpus, sizes[i]), nthreads=threads)
+        cpu_el += 1 << sizes[i]
+    t_cpu = time.perf_counter() - t0
     return {"jobs": njobs, "elements": total, "log_n_range": [lo, hi],
+            "verified": verified, "verified_jobs": len(sample),
+            "verified_how": "seeded sample covering every size class, after the first batched launch, "
+                            "bit-exact against gsn_ntt (the per-call path) on a copy of the same input",
+            "cpu_port": {"Melem_s": round(cpu_el / t_cpu / 1e6, 4) if t_cpu > 0 else None, "jobs": len(cpu_jobs),
+                         "elements": cpu_el, "cores": threads, "kind": "port",
+                         "sample": "the verified jobs up to 2^16, restated host FFT each"},
             "batched_ms": round(t_batch * 1e3, 3), "per_call_ms": round(t_call * 1e3, 3),
             "batched_Melem_s": round(total / t_batch / 1e6, 1), "per_call_Melem_s": round(total / t_call / 1e6, 1),
             "speedup": round(t_call / t_batch, 3), "batched_imad_T_s": round(work / t_batch / 1e12, 3),
@@ -449,10 +597,7 @@ def run_gpu(args, rank, local, ws):
         "metric": METRIC, "value": round(value, 3), "unit": "Melem/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(t_step * 1e3, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-        "config": {"workload": "forward NTT, MNT4-753 scalar field r (24 limbs), n=2^18, per GPU",
-                   "field": "mnt4753_fr", "log_n": log_n, "elements_per_step": n,
-                   "l2": "flushed (256 MB write) before each step; input 25 MB < L2",
-                   "parallelism": f"replicas x{ws}"},
+        "config": headline_config(ws),
         "e2e": {"value": round(n * ws / e2e_t / 1e6, 3), "unit": "Melem/s", "h2d_bytes_per_step": nbytes,
                 "d2h_bytes_per_step": nbytes,
                 "api": "gsn_ntt_host_batch over one pinned host buffer per step: each step's input copied in "
@@ -481,7 +626,10 @@ def run_gpu(args, rank, local, ws):
         t20, _ = time_device_ntt(g, torch, f, 20, 3, 1, flush=flush)
         extra["mnt4753_fr_2^20"] = {"ms": round(float(np.median(t20)) * 1e3, 3),
                                     "imad_frac": round(imad_work(f, 20) / float(np.median(t20)) / ip["mads_per_s"], 4)}
+        extra["mnt4753_fr_2^20"]["cpu_port"] = cpu_port_rate(2, 20, f.device_random(1 << 20, SEED + 20))
+        extra["p32_2^16"] = config1_p32_2_16(g, torch, flush, hbm_gbs)
         extra["p32_sweep"] = p32_sweep(g, torch, flush, hbm_gbs)
+        extra["poly_product_2^21"] = poly_product_2_21(g, torch)
         extra["hbm_peak_gbs"] = hbm_gbs
         try:
             extra["bls12_381_batch_4096"] = batch_vs_per_call(g, torch)
@@ -579,8 +727,7 @@ def run_reference(args, rank, ws):
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": "Melem/s", "n_gpus": ws,
             "steps": len(ts), "warmup": args.warmup, "ms_per_step": round(t * 1e3, 3),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
-            "config": {"workload": "forward NTT, MNT4-753 scalar field r (24 limbs), n=2^18",
-                       "field": "mnt4753_fr", "log_n": HEADLINE_LOG_N},
+            "config": headline_config(ws),
             "cpu_baseline": cb,
             "e2e": {"value": v, "unit": "Melem/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 

@@ -118,39 +118,6 @@ __device__ __forceinline__ uint32_t sub1(uint32_t a, uint32_t b) {
   return (a < b) ? r + p : r;
 }
 
-// The same three operations with the "+p if it went negative" correction as a borrow mask and one
-// multiply-add: sub.cc / subc give mask = 0 or 0xFFFFFFFF, and r + mask * (2^32 - p) adds p exactly
-// when the mask is set.  The correction then runs on the multiply-add pipe instead of a compare and
-// a select on the integer ALU pipe, which the one-limb butterfly otherwise saturates.
-template <class P>
-__device__ __forceinline__ uint32_t fix_borrow1(uint32_t r, uint32_t mask) {
-  return r + mask * (0u - P::mod(0));
-}
-template <class P>
-__device__ __forceinline__ uint32_t mul1_m(uint32_t a, uint32_t b) {
-  constexpr uint32_t p = P::mod(0);
-  constexpr uint32_t pinv_pos = 0u - P::PINV;
-  const uint32_t hi = ptx::mul_hi(a, b);
-  const uint32_t m = (a * b) * pinv_pos;
-  const uint32_t mh = ptx::mul_hi(m, p);
-  uint32_t r, mask;
-  asm("sub.cc.u32 %0, %2, %3;\n\tsubc.u32 %1, 0, 0;" : "=r"(r), "=r"(mask) : "r"(hi), "r"(mh));
-  return fix_borrow1<P>(r, mask);
-}
-template <class P>
-__device__ __forceinline__ uint32_t add1_m(uint32_t a, uint32_t b) {
-  const uint32_t t = P::mod(0) - b;  // in [1, p]; a - t = a + b - p
-  uint32_t r, mask;
-  asm("sub.cc.u32 %0, %2, %3;\n\tsubc.u32 %1, 0, 0;" : "=r"(r), "=r"(mask) : "r"(a), "r"(t));
-  return fix_borrow1<P>(r, mask);
-}
-template <class P>
-__device__ __forceinline__ uint32_t sub1_m(uint32_t a, uint32_t b) {
-  uint32_t r, mask;
-  asm("sub.cc.u32 %0, %2, %3;\n\tsubc.u32 %1, 0, 0;" : "=r"(r), "=r"(mask) : "r"(a), "r"(b));
-  return fix_borrow1<P>(r, mask);
-}
-
 // ---------------------------------------------------------------------------
 // Multi-limb fields, one element per thread.
 // ---------------------------------------------------------------------------

@@ -1,7 +1,7 @@
 // Autotuner: per (field, log n), time candidate plans on the current device
 // and keep the fastest; persist the table as JSON.  (No reference
 // counterpart: the reference hard-codes 1024 chunks of 64 points,
-// cuda/fft_kernel.cu:56-59.)
+// cuda/fft_kernel.cu:29-32,57.)
 //
 // Candidates vary the pass count / radix split, the tile width (columns per
 // tile), the threads per CTA and, for the 32-bit field, the register-blocked

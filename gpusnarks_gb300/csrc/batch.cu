@@ -1,6 +1,6 @@
 // Batched transforms: many independent NTTs of uneven power-of-two sizes in
 // one persistent launch fed by a device work queue, optionally captured into
-// a CUDA graph.  (No reference counterpart: cuda/fft_kernel.cu:144-174 runs
+// a CUDA graph.  (No reference counterpart: cuda/fft_kernel.cu:117-147 runs
 // one fixed-size transform per call.)
 //
 // Work queue: one 64-bit item per tile, job << 32 | pass << 28 | tile,

@@ -1,14 +1,14 @@
 // gsn_ntt_noalloc: an NTT entry point that allocates no device memory.
 //
 // Who needs it: callers that must not call cudaMalloc / cudaFree at the
-// moment they run a transform -- code recording a CUDA stream capture (an
-// allocation there breaks the capture), latency-critical loops where an
+// moment they run a transform -- latency-critical loops where an
 // allocation's implicit device synchronisation is not acceptable, and
 // embedders whose memory is owned by another allocator so they cannot hand
 // this library its own device buffers.  gsn_ntt draws the scratch buffer its
 // multi-pass plans need from a per-stream pool that it grows with cudaMalloc;
 // this entry point instead uses one fixed scratch array compiled into the
-// library.
+// library.  It runs the generic multi-pass kernel for every field (p32
+// included), which needs only the full twiddle table gsn_prepare builds.
 //
 // The array: kNoAllocScratchBytes (64 MiB) of __device__ memory in this file.
 // Every GPU that loads the library holds it until the process exits.  A

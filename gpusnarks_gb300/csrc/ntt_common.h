@@ -26,6 +26,11 @@
 
 namespace gsn {
 
+// Current device and its SM count (looked up once per device; defined in runtime.cu).  Grids of the
+// grid-stride kernels are capped at a multiple of the SM count.
+int current_device();
+int current_device_sms();
+
 constexpr int kMaxPasses = 4;
 constexpr int kMaxLimbs = 24;
 

@@ -1,7 +1,7 @@
 // NTT kernels, templated on the field.  Included by one .cu per field so the
 // fields compile in parallel.
 //
-// Replaces cuda_fft (cuda/fft_kernel.cu:79-142).  The reference launches 1280
+// Replaces cuda_fft (cuda/fft_kernel.cu:52-115).  The reference launches 1280
 // threads that each run a 1024-term direct sum and a 64-point radix-2 loop in
 // local memory (O(n * 1024) products); here each pass is a radix-2^r
 // sub-transform of a shared-memory tile (see ntt_common.h for the
@@ -425,6 +425,9 @@ __global__ void __maxnreg__(batch_max_regs<P>())
 }
 
 // --- host-side launchers, instantiated per field ---------------------------
+// Elementwise grid-stride kernels launch at most this many CTAs per SM.
+constexpr uint64_t kGridPerSm = 64;
+
 template <class P>
 struct Kernels {
   static cudaError_t pass(const PassArgs& A, int block, cudaStream_t s) {
@@ -468,7 +471,7 @@ struct Kernels {
   static cudaError_t convert(uint32_t* data, uint64_t n, int mode, cudaStream_t s) {
     const int block = 256;
     uint64_t grid = (n + block - 1) / block;
-    if (grid > 152 * 64) grid = 152 * 64;
+    if (grid > kGridPerSm * (uint64_t)current_device_sms()) grid = kGridPerSm * (uint64_t)current_device_sms();
     if (grid == 0) return cudaSuccess;
     convert_kernel<P><<<(unsigned)grid, block, 0, s>>>(data, n, mode);
     return cudaGetLastError();
@@ -476,7 +479,7 @@ struct Kernels {
   static cudaError_t fill(uint32_t* out, uint64_t n, uint64_t seed, cudaStream_t s) {
     const int block = 256;
     uint64_t grid = (n + block - 1) / block;
-    if (grid > 152 * 64) grid = 152 * 64;
+    if (grid > kGridPerSm * (uint64_t)current_device_sms()) grid = kGridPerSm * (uint64_t)current_device_sms();
     if (grid == 0) return cudaSuccess;
     fill_random_kernel<P><<<(unsigned)grid, block, 0, s>>>(out, n, seed);
     return cudaGetLastError();
@@ -484,7 +487,7 @@ struct Kernels {
   static cudaError_t pointwise(uint32_t* a, const uint32_t* b, uint64_t n, cudaStream_t s) {
     const int block = 256;
     uint64_t grid = (n + block - 1) / block;
-    if (grid > 152 * 64) grid = 152 * 64;
+    if (grid > kGridPerSm * (uint64_t)current_device_sms()) grid = kGridPerSm * (uint64_t)current_device_sms();
     pointwise_mul_kernel<P><<<(unsigned)grid, block, 0, s>>>(a, b, n);
     return cudaGetLastError();
   }
@@ -494,7 +497,7 @@ struct Kernels {
     for (int i = 0; i < P::N; ++i) z.l[i] = zr2[i];
     const int block = 256;
     uint64_t grid = (n + block - 1) / block;
-    if (grid > 152 * 64) grid = 152 * 64;
+    if (grid > kGridPerSm * (uint64_t)current_device_sms()) grid = kGridPerSm * (uint64_t)current_device_sms();
     if (grid == 0) return cudaSuccess;
     coset_quotient_kernel<P><<<(unsigned)grid, block, 0, s>>>(a, b, c, n, z);
     return cudaGetLastError();

@@ -300,7 +300,8 @@ extern "C" int gsn_fft_ref_compat(uint32_t* data, uint32_t log_n, const uint32_t
   refc::phase1_kernel<<<grid, block, 0, s>>>(data, tmp, (int)log_n, log_cpus, w);
   refc::phase2_kernel<<<grid, block, 0, s>>>(tmp, (int)log_n, log_cpus, w);
   const uint64_t n = 1ull << log_n;
-  const unsigned g3 = (unsigned)((n + 255) / 256 < 152 * 8 ? (n + 255) / 256 : 152 * 8);
+  const uint64_t g3_cap = 8 * (uint64_t)current_device_sms();
+  const unsigned g3 = (unsigned)((n + 255) / 256 < g3_cap ? (n + 255) / 256 : g3_cap);
   refc::phase3_kernel<<<g3, 256, 0, s>>>(data, tmp, (int)log_n, log_cpus);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "reference-compatible launch");

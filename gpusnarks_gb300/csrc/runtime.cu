@@ -1,6 +1,6 @@
 // Runtime and C ABI for single transforms.
 //
-// Replaces the host launcher best_fft (cuda/fft_kernel.cu:144-174): that one
+// Replaces the host launcher best_fft (cuda/fft_kernel.cu:117-147): that one
 // prints, asserts n == 2^16, ignores omg, cudaMallocs two buffers per call
 // that it never frees, launches one fixed <<<5,256>>> grid and exits the
 // process on a launch error.  Here a call validates its arguments, resolves
@@ -45,6 +45,32 @@ int cuda_fail(cudaError_t e, const char* what) {
 
 static std::atomic<uint64_t> g_launches{0};
 void count_launches(uint64_t n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+int current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return dev;
+}
+
+// SM count of the current device, looked up once per device.
+int current_device_sms() {
+  constexpr int kDevices = 64;
+  static std::atomic<int> sms[kDevices];
+  const int dev = current_device();
+  if (dev < 0 || dev >= kDevices) return 1;
+  int v = sms[dev].load(std::memory_order_relaxed);
+  if (v <= 0) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0) {
+      cudaGetLastError();
+      v = 1;
+    }
+    sms[dev].store(v, std::memory_order_relaxed);
+  }
+  return v;
+}
 
 const FieldOps* field_ops(int field) {
   switch (field) {
@@ -226,12 +252,14 @@ struct DevBuf {
   size_t bytes = 0;
 };
 
+// Every entry belongs to the device that was current when it was built: tables and scratch are keyed by
+// device as well, so a process that drives several GPUs never hands one GPU another's memory.
 struct TableCache {
   std::mutex mu;
-  // (field, tw_log, root limbs) -> powers of the root
-  std::map<std::tuple<int, int, std::string>, DevBuf> powers;
-  std::map<cudaStream_t, DevBuf> scratch;
-  cudaStream_t gen_stream = nullptr;
+  // (device, field, tw_log, root limbs) -> powers of the root
+  std::map<std::tuple<int, int, int, std::string>, DevBuf> powers;
+  std::map<std::pair<int, cudaStream_t>, DevBuf> scratch;
+  std::map<int, cudaStream_t> gen_stream;  // per device
 };
 
 static TableCache& cache() {
@@ -263,21 +291,23 @@ static void default_root(const FieldOps& F, int log_n, uint32_t* out) {
 // on first use.  Caller holds no lock.
 static int powers_table(const FieldOps& F, const uint32_t* base, int log_count, const uint32_t** out) {
   TableCache& C = cache();
+  const int dev = current_device();
   std::lock_guard<std::mutex> g(C.mu);
-  auto key = std::make_tuple(F.id, log_count, limbs_key(base, F.limbs));
+  auto key = std::make_tuple(dev, F.id, log_count, limbs_key(base, F.limbs));
   auto it = C.powers.find(key);
   if (it != C.powers.end()) {
     *out = static_cast<const uint32_t*>(it->second.p);
     return GSN_OK;
   }
-  if (!C.gen_stream) GSN_CUDA(cudaStreamCreateWithFlags(&C.gen_stream, cudaStreamNonBlocking));
+  cudaStream_t& gen = C.gen_stream[dev];
+  if (!gen) GSN_CUDA(cudaStreamCreateWithFlags(&gen, cudaStreamNonBlocking));
   const uint64_t count = (uint64_t)1 << log_count;
   DevBuf b;
   b.bytes = count * F.limbs * sizeof(uint32_t);
   int rc = dev_alloc(&b.p, b.bytes);
   if (rc) return rc;
-  cudaError_t e = F.powers(static_cast<uint32_t*>(b.p), count, base, C.gen_stream);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(C.gen_stream);
+  cudaError_t e = F.powers(static_cast<uint32_t*>(b.p), count, base, gen);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(gen);
   if (e != cudaSuccess) {
     dev_free(b.p);
     return cuda_fail(e, "twiddle generation");
@@ -292,20 +322,7 @@ static int powers_table(const FieldOps& F, const uint32_t* base, int log_count, 
 // order >= 2^log_n (its powers include every smaller root's), else build one
 // of order 2^max(log_n, default_tw_log).
 static int default_twiddles(const FieldOps& F, int log_n, const uint32_t** tw, int* tw_log) {
-  {
-    TableCache& C = cache();
-    std::lock_guard<std::mutex> g(C.mu);
-    for (int k = log_n; k <= F.max_log_n; ++k) {
-      uint32_t r[kMaxLimbs];
-      default_root(F, k, r);
-      auto it = C.powers.find(std::make_tuple(F.id, k, limbs_key(r, F.limbs)));
-      if (it != C.powers.end()) {
-        *tw = static_cast<const uint32_t*>(it->second.p);
-        *tw_log = k;
-        return GSN_OK;
-      }
-    }
-  }
+  if (find_default_twiddles(F, log_n, tw, tw_log)) return GSN_OK;
   const int k = std::min(F.max_log_n, std::max(log_n, F.default_tw_log));
   uint32_t r[kMaxLimbs];
   default_root(F, k, r);
@@ -374,11 +391,12 @@ int resolve_tables(const FieldOps& F, uint32_t log_n, const uint32_t* omega, int
 
 bool find_default_twiddles(const FieldOps& F, int log_n, const uint32_t** tw, int* tw_log) {
   TableCache& C = cache();
+  const int dev = current_device();
   std::lock_guard<std::mutex> g(C.mu);
   for (int k = log_n; k <= F.max_log_n; ++k) {
     uint32_t r[kMaxLimbs];
     default_root(F, k, r);
-    auto it = C.powers.find(std::make_tuple(F.id, k, limbs_key(r, F.limbs)));
+    auto it = C.powers.find(std::make_tuple(dev, F.id, k, limbs_key(r, F.limbs)));
     if (it != C.powers.end()) {
       *tw = static_cast<const uint32_t*>(it->second.p);
       *tw_log = k;
@@ -410,8 +428,9 @@ int resolve_p32_tables(const FieldOps& F, const Plan& plan, Tables* T) {
 
 int scratch_for(cudaStream_t s, size_t bytes, uint32_t** out) {
   TableCache& C = cache();
+  const int dev = current_device();
   std::lock_guard<std::mutex> g(C.mu);
-  DevBuf& b = C.scratch[s];
+  DevBuf& b = C.scratch[std::make_pair(dev, s)];
   if (b.bytes < bytes) {
     if (b.p) {
       GSN_CUDA(cudaStreamSynchronize(s));
@@ -428,13 +447,7 @@ int scratch_for(cudaStream_t s, size_t bytes, uint32_t** out) {
 }
 
 static int enqueue_p32(const Plan& plan, const Tables& T, uint32_t* data, uint32_t* scratch, cudaStream_t s) {
-  static int sms = 0;
-  if (!sms) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (sms <= 0) sms = 152;
-  }
+  const int sms = current_device_sms();
   P32Args A;
   std::memset(&A, 0, sizeof(A));
   A.tw_lo = T.p32_lo;
@@ -584,11 +597,78 @@ static int quotient_impl(int field, uint32_t* a, const uint32_t* b, const uint32
   return GSN_OK;
 }
 
-static std::mutex g_host_mu;
-// device buffers of the host-memory entry points (gsn_ntt_host, gsn_ntt_host_batch), guarded by g_host_mu and
-// freed by gsn_release_caches
-static DevBuf g_host_single;
-static DevBuf g_host_pipe[3];
+// Device buffers, streams and events of the host-memory entry points (gsn_ntt_host, gsn_ntt_host_batch).  A
+// call checks one state out of an idle pool for the current device (or makes a new one) and returns it when
+// done, so concurrent callers on different host threads each run on their own buffers and streams and none
+// waits for another.  gsn_release_caches frees the idle states.
+struct HostState {
+  static constexpr int kBufs = 3;
+  int dev = 0;
+  cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
+  cudaEvent_t ev_in[kBufs] = {}, ev_comp[kBufs] = {}, ev_out[kBufs] = {};
+  DevBuf bufs[kBufs];
+};
+
+static std::mutex g_host_pool_mu;
+static std::vector<HostState*> g_host_idle;
+
+static void host_state_destroy(HostState* h) {
+  for (DevBuf& b : h->bufs) dev_free(b.p);
+  for (cudaStream_t s : {h->s_in, h->s_comp, h->s_out})
+    if (s) cudaStreamDestroy(s);
+  for (int b = 0; b < HostState::kBufs; ++b)
+    for (cudaEvent_t e : {h->ev_in[b], h->ev_comp[b], h->ev_out[b]})
+      if (e) cudaEventDestroy(e);
+  delete h;
+}
+
+static int host_state_acquire(HostState** out) {
+  const int dev = current_device();
+  {
+    std::lock_guard<std::mutex> g(g_host_pool_mu);
+    for (size_t i = 0; i < g_host_idle.size(); ++i) {
+      if (g_host_idle[i]->dev == dev) {
+        *out = g_host_idle[i];
+        g_host_idle.erase(g_host_idle.begin() + (long)i);
+        return GSN_OK;
+      }
+    }
+  }
+  HostState* h = new HostState();
+  h->dev = dev;
+  cudaError_t e = cudaSuccess;
+  for (cudaStream_t* s : {&h->s_in, &h->s_comp, &h->s_out})
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
+  for (int b = 0; b < HostState::kBufs && e == cudaSuccess; ++b)
+    for (cudaEvent_t* ev : {&h->ev_in[b], &h->ev_comp[b], &h->ev_out[b]})
+      if (e == cudaSuccess) e = cudaEventCreateWithFlags(ev, cudaEventDisableTiming);
+  if (e != cudaSuccess) {
+    host_state_destroy(h);
+    return cuda_fail(e, "host-path stream and event creation");
+  }
+  *out = h;
+  return GSN_OK;
+}
+
+static void host_state_release(HostState* h) {
+  std::lock_guard<std::mutex> g(g_host_pool_mu);
+  g_host_idle.push_back(h);
+}
+
+// Grows buffer k of a checked-out state to `bytes` (after the state's streams have drained).
+static int host_state_buffer(HostState* h, int k, size_t bytes) {
+  DevBuf& b = h->bufs[k];
+  if (b.bytes >= bytes) return GSN_OK;
+  GSN_CUDA(cudaStreamSynchronize(h->s_out));
+  GSN_CUDA(cudaStreamSynchronize(h->s_comp));
+  dev_free(b.p);
+  b.p = nullptr;
+  b.bytes = 0;
+  int rc = dev_alloc(&b.p, bytes);
+  if (rc) return rc;
+  b.bytes = bytes;
+  return GSN_OK;
+}
 }  // namespace gsn
 
 using namespace gsn;
@@ -649,28 +729,52 @@ int gsn_ntt_host(int field, uint32_t* data, uint32_t log_n, const uint32_t* omeg
   if (!data) return set_error(GSN_ERR_ARG, "null data pointer");
   if ((int)log_n > std::min(F->max_log_n, F->two_adicity))
     return set_error(GSN_ERR_SIZE, "log_n=%u exceeds the limit for field %d", log_n, field);
-  std::lock_guard<std::mutex> g(g_host_mu);
-  static cudaStream_t stream = nullptr;
-  DevBuf& buf = g_host_single;
-  if (!stream) GSN_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  HostState* h = nullptr;
+  int rc = host_state_acquire(&h);
+  if (rc) return rc;
   const size_t bytes = ((size_t)1 << log_n) * F->limbs * sizeof(uint32_t);
-  if (buf.bytes < bytes) {
-    dev_free(buf.p);
-    buf.p = nullptr;
-    buf.bytes = 0;
-    int rc = dev_alloc(&buf.p, bytes);
+  rc = host_state_buffer(h, 0, bytes);
+  if (!rc) {
+    uint32_t* dev = static_cast<uint32_t*>(h->bufs[0].p);
+    const cudaStream_t stream = h->s_comp;
+    cudaError_t e = cudaMemcpyAsync(dev, data, bytes, cudaMemcpyHostToDevice, stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "host-to-device copy");
+    if (!rc) rc = ntt_impl(field, dev, log_n, omega, dir, shift, nullptr, stream);
+    if (!rc) {
+      e = cudaMemcpyAsync(data, dev, bytes, cudaMemcpyDeviceToHost, stream);
+      if (e != cudaSuccess) rc = cuda_fail(e, "device-to-host copy");
+    }
+    e = cudaStreamSynchronize(stream);
+    if (!rc && e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize");
+  }
+  host_state_release(h);
+  return rc;
+}
+
+// Copies of array i+1 (in) and i-1 (out) overlap the transform of array i: three device buffers in
+// rotation, copy-in, transform and copy-out on their own streams, ordered by events.
+static int host_batch_run(HostState* h, const FieldOps* F, int field, uint32_t* const* data, size_t count,
+                          uint32_t log_n, const uint32_t* omega, int dir, const uint32_t* shift) {
+  constexpr int kBufs = HostState::kBufs;
+  const size_t bytes = ((size_t)1 << log_n) * F->limbs * sizeof(uint32_t);
+  for (int k = 0; k < kBufs; ++k) {
+    int rc = host_state_buffer(h, k, bytes);
     if (rc) return rc;
-    buf.bytes = bytes;
   }
-  uint32_t* dev = static_cast<uint32_t*>(buf.p);
-  GSN_CUDA(cudaMemcpyAsync(dev, data, bytes, cudaMemcpyHostToDevice, stream));
-  int rc = ntt_impl(field, dev, log_n, omega, dir, shift, nullptr, stream);
-  if (rc) {
-    cudaStreamSynchronize(stream);
-    return rc;
+  for (size_t i = 0; i < count; ++i) {
+    const int b = (int)(i % kBufs);
+    uint32_t* dev = static_cast<uint32_t*>(h->bufs[b].p);
+    if (i >= kBufs) GSN_CUDA(cudaStreamWaitEvent(h->s_in, h->ev_out[b], 0));  // array i-3 has left this buffer
+    GSN_CUDA(cudaMemcpyAsync(dev, data[i], bytes, cudaMemcpyHostToDevice, h->s_in));
+    GSN_CUDA(cudaEventRecord(h->ev_in[b], h->s_in));
+    GSN_CUDA(cudaStreamWaitEvent(h->s_comp, h->ev_in[b], 0));
+    int rc = ntt_impl(field, dev, log_n, omega, dir, shift, nullptr, h->s_comp);
+    if (rc) return rc;
+    GSN_CUDA(cudaEventRecord(h->ev_comp[b], h->s_comp));
+    GSN_CUDA(cudaStreamWaitEvent(h->s_out, h->ev_comp[b], 0));
+    GSN_CUDA(cudaMemcpyAsync(data[i], dev, bytes, cudaMemcpyDeviceToHost, h->s_out));
+    GSN_CUDA(cudaEventRecord(h->ev_out[b], h->s_out));
   }
-  GSN_CUDA(cudaMemcpyAsync(data, dev, bytes, cudaMemcpyDeviceToHost, stream));
-  GSN_CUDA(cudaStreamSynchronize(stream));
   return GSN_OK;
 }
 
@@ -684,57 +788,17 @@ int gsn_ntt_host_batch(int field, uint32_t* const* data, size_t count, uint32_t 
   if ((int)log_n > std::min(F->max_log_n, F->two_adicity))
     return set_error(GSN_ERR_SIZE, "log_n=%u exceeds the limit for field %d", log_n, field);
   if (count == 0) return GSN_OK;
-  std::lock_guard<std::mutex> g(g_host_mu);
-  // three device buffers in rotation; copy-in, transform and copy-out on their own streams, ordered by
-  // events, so array i+1 uploads and array i-1 downloads while array i is transformed
-  constexpr int kBufs = 3;
-  static cudaStream_t s_in = nullptr, s_comp = nullptr, s_out = nullptr;
-  DevBuf* const bufs = g_host_pipe;
-  static cudaEvent_t ev_in[kBufs], ev_comp[kBufs], ev_out[kBufs];
-  if (!s_in) {
-    GSN_CUDA(cudaStreamCreateWithFlags(&s_in, cudaStreamNonBlocking));
-    GSN_CUDA(cudaStreamCreateWithFlags(&s_comp, cudaStreamNonBlocking));
-    GSN_CUDA(cudaStreamCreateWithFlags(&s_out, cudaStreamNonBlocking));
-    for (int b = 0; b < kBufs; ++b) {
-      GSN_CUDA(cudaEventCreateWithFlags(&ev_in[b], cudaEventDisableTiming));
-      GSN_CUDA(cudaEventCreateWithFlags(&ev_comp[b], cudaEventDisableTiming));
-      GSN_CUDA(cudaEventCreateWithFlags(&ev_out[b], cudaEventDisableTiming));
-    }
+  HostState* h = nullptr;
+  int rc = host_state_acquire(&h);
+  if (rc) return rc;
+  rc = host_batch_run(h, F, field, data, count, log_n, omega, dir, shift);
+  // drain all three streams, also after a failure, before the state goes back to the pool
+  for (cudaStream_t s : {h->s_in, h->s_comp, h->s_out}) {
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (!rc && e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize");
   }
-  const size_t bytes = ((size_t)1 << log_n) * F->limbs * sizeof(uint32_t);
-  for (int k = 0; k < kBufs; ++k) {
-    DevBuf& b = bufs[k];
-    if (b.bytes < bytes) {
-      GSN_CUDA(cudaStreamSynchronize(s_out));  // earlier batches are done with it
-      dev_free(b.p);
-      b.p = nullptr;
-      b.bytes = 0;
-      int rc = dev_alloc(&b.p, bytes);
-      if (rc) return rc;
-      b.bytes = bytes;
-    }
-  }
-  for (size_t i = 0; i < count; ++i) {
-    const int b = (int)(i % kBufs);
-    uint32_t* dev = static_cast<uint32_t*>(bufs[b].p);
-    if (i >= kBufs) GSN_CUDA(cudaStreamWaitEvent(s_in, ev_out[b], 0));  // array i-3 has left this buffer
-    GSN_CUDA(cudaMemcpyAsync(dev, data[i], bytes, cudaMemcpyHostToDevice, s_in));
-    GSN_CUDA(cudaEventRecord(ev_in[b], s_in));
-    GSN_CUDA(cudaStreamWaitEvent(s_comp, ev_in[b], 0));
-    int rc = ntt_impl(field, dev, log_n, omega, dir, shift, nullptr, s_comp);
-    if (rc) {
-      cudaStreamSynchronize(s_in);
-      cudaStreamSynchronize(s_comp);
-      cudaStreamSynchronize(s_out);
-      return rc;
-    }
-    GSN_CUDA(cudaEventRecord(ev_comp[b], s_comp));
-    GSN_CUDA(cudaStreamWaitEvent(s_out, ev_comp[b], 0));
-    GSN_CUDA(cudaMemcpyAsync(data[i], dev, bytes, cudaMemcpyDeviceToHost, s_out));
-    GSN_CUDA(cudaEventRecord(ev_out[b], s_out));
-  }
-  GSN_CUDA(cudaStreamSynchronize(s_out));
-  return GSN_OK;
+  host_state_release(h);
+  return rc;
 }
 
 int gsn_prepare(int field, uint32_t log_n, const uint32_t* omega) {
@@ -813,15 +877,14 @@ int gsn_host_free(void* ptr) {
 }
 
 int gsn_release_caches(void) {
-  std::lock_guard<std::mutex> gh(g_host_mu);  // same order as the host entry points: host lock, then cache
+  GSN_CUDA(cudaDeviceSynchronize());
+  {
+    std::lock_guard<std::mutex> gh(g_host_pool_mu);
+    for (HostState* h : g_host_idle) host_state_destroy(h);
+    g_host_idle.clear();
+  }
   TableCache& C = cache();
   std::lock_guard<std::mutex> g(C.mu);
-  GSN_CUDA(cudaDeviceSynchronize());
-  for (DevBuf* b : {&g_host_single, &g_host_pipe[0], &g_host_pipe[1], &g_host_pipe[2]}) {
-    dev_free(b->p);
-    b->p = nullptr;
-    b->bytes = 0;
-  }
   for (auto& kv : C.powers) dev_free(kv.second.p);
   C.powers.clear();
   for (auto& kv : C.scratch) dev_free(kv.second.p);

@@ -19,7 +19,7 @@ Fields:
 The generator of each NTT field is a quadratic non-residue, so
 ``g^((p-1)/2^k)`` has exact order ``2^k`` for every ``k`` up to the 2-adicity.
 The reference ships no generator and ignores the ``omg`` argument of
-``best_fft`` (cuda/fft_kernel.cu:144-162); these are this library's choices.
+``best_fft`` (cuda/fft_kernel.cu:117-147; the kernel uses the raw modulus limbs, :65-68); these are this library's choices.
 """
 from __future__ import annotations
 

@@ -149,6 +149,33 @@ def poisson_trace(count: int, rate: float, seed: int, fields=(1, 2), lo=12, hi=2
     return [(float(t[i]), int(fs[i]), int(ks[i]), int(ds[i])) for i in range(count)]
 
 
+def verification_sample(trace, seed: int, count: int = 48, max_bytes: int = 2 << 30) -> list[int]:
+    """Indices of a seeded sample of trace requests whose outputs are checked: the largest request of
+    each field and one of each (field, direction) pair first, then random ones, at most `count` requests
+    and `max_bytes` of output in total."""
+    from . import BY_ID
+    rng = np.random.default_rng(seed + 1)
+    size = [(1 << k) * BY_ID[fid].limbs * 4 for _, fid, k, _ in trace]
+    must: list[int] = []
+    for fid in sorted({e[1] for e in trace}):
+        idx = [i for i, e in enumerate(trace) if e[1] == fid]
+        must.append(max(idx, key=lambda i: (trace[i][2], -i)))
+        for d in sorted({trace[i][3] for i in idx}):
+            cand = [i for i in idx if trace[i][3] == d]
+            must.append(int(rng.choice(cand)))
+    rest = [int(i) for i in rng.permutation(len(trace))]
+    out: list[int] = []
+    total = 0
+    for i in must + rest:
+        if i in out or len(out) >= count:
+            continue
+        if total + size[i] > max_bytes and i not in must:
+            continue
+        out.append(i)
+        total += size[i]
+    return sorted(out)
+
+
 def bench_serving(g, torch, *, seconds: float = 1.0, rate: float = 2000.0, budget_gb: float = 120.0,
                   max_inflight: int = 4, seed: int = 0x5EED0005, policy: int = OLDEST_FIRST) -> dict:
     """The mixed serving stream: Poisson arrivals at `rate` req/s for `seconds`, BLS12-381 / MNT4-753
@@ -156,7 +183,8 @@ def bench_serving(g, torch, *, seconds: float = 1.0, rate: float = 2000.0, budge
     from . import BY_ID
     trace = poisson_trace(max(1, int(rate * seconds)), rate, seed)
     # one pinned input and output buffer per (field, size): inputs are uniform
-    # random elements; outputs of equal-shape requests overwrite each other
+    # random elements; outputs of equal-shape requests overwrite each other,
+    # except for a seeded sample of requests (below) that get their own output
     bufs = {}
     for _, fid, k, _ in trace:
         if (fid, k) not in bufs:
@@ -167,6 +195,7 @@ def bench_serving(g, torch, *, seconds: float = 1.0, rate: float = 2000.0, budge
             a = np.ctypeslib.as_array(ctypes.cast(pin, ctypes.POINTER(ctypes.c_uint32)), shape=((1 << k) * f.limbs,))
             a[:] = f.device_random(1 << k, seed + 97 * k + fid).reshape(-1)
             bufs[(fid, k)] = (pin, pout)
+    own: dict[int, ctypes.c_void_p] = {}  # sampled requests' own output buffers
     srv = Server(int(budget_gb * (1 << 30)), max_inflight=max_inflight, policy=policy)
     try:
         for fid in (1, 2):
@@ -175,17 +204,37 @@ def bench_serving(g, torch, *, seconds: float = 1.0, rate: float = 2000.0, budge
         # buffer runs far below the link rate, and a serving process reuses its buffers
         srv.run_trace([TraceEntry(0.0, Request(fid, k, 0, None, pin.value, pout.value))
                        for (fid, k), (pin, pout) in bufs.items()])
+        sample = verification_sample(trace, seed)
+        for i in sample:
+            _, fid, k, _ = trace[i]
+            own[i] = g.host_buffer((1 << k) * BY_ID[fid].limbs * 4)
         entries = []
-        for (t, fid, k, d) in trace:
+        for i, (t, fid, k, d) in enumerate(trace):
             pin, pout = bufs[(fid, k)]
-            entries.append(TraceEntry(t, Request(fid, k, d, None, pin.value, pout.value)))
+            out = own[i] if i in own else pout
+            entries.append(TraceEntry(t, Request(fid, k, d, None, pin.value, out.value)))
         lat, makespan, ph = srv.run_trace(entries, phases=True)
         st = srv.stats()
+        # every sampled output against the plain path (gsn_ntt on the same input, same direction)
+        verified = True
+        for i in sample:
+            _, fid, k, d = trace[i]
+            f = BY_ID[fid]
+            shape = ((1 << k) * f.limbs,)
+            pin, _ = bufs[(fid, k)]
+            x = np.ctypeslib.as_array(ctypes.cast(pin, ctypes.POINTER(ctypes.c_uint32)), shape=shape).copy()
+            got = np.ctypeslib.as_array(ctypes.cast(own[i], ctypes.POINTER(ctypes.c_uint32)), shape=shape)
+            t = g.to_device(x)
+            g.ntt(f, t, direction=d)
+            verified = verified and bool(np.array_equal(g.to_host(t), got))
+            del t
     finally:
         srv.close()
         for pin, pout in bufs.values():
             g.free_host_buffer(pin)
             g.free_host_buffer(pout)
+        for b in own.values():
+            g.free_host_buffer(b)
     elements = sum(1 << k for _, _, k, _ in trace)
     return {"requests": len(trace), "rate_req_s": rate, "arrival_window_s": round(trace[-1][0], 4),
             "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
@@ -200,5 +249,8 @@ def bench_serving(g, torch, *, seconds: float = 1.0, rate: float = 2000.0, budge
             "phase_ms_p99": {k: round(float(np.percentile(ph[:, i], 99)) * 1e3, 3) for i, k in enumerate(PHASES)},
             "p99_request_phases_ms": {k: round(float(ph[int(np.argsort(lat)[int(0.99 * (len(lat) - 1))]), i]) * 1e3, 3)
                                       for i, k in enumerate(PHASES)},
+            "verified": verified, "verified_requests": len(sample),
+            "verified_how": "a seeded sample (both fields, every direction, the largest size of each field) "
+                            "with their own output buffers, bit-exact against gsn_ntt on the same input",
             "budget_bytes": int(budget_gb * (1 << 30)), "max_inflight": max_inflight,
             "policy": "least_work_first" if policy == LEAST_WORK_FIRST else "oldest_first"}

@@ -25,12 +25,12 @@
  *
  * Reference interfaces replaced:
  *   best_fft<FieldT>(std::vector<FieldT>&, const FieldT& omg)
- *       cuda/fft_kernel.h:24-25, cuda/fft_kernel.cu:144-174
+ *       cuda/fft_kernel.h:24-25, cuda/fft_kernel.cu:117-147
  *       -> gsn_ntt_host (and the C++ shim include/gsn_best_fft.h)
- *   the device launch inside it (cuda_fft<<<blocks,threads>>>, :162)
+ *   the device launch inside it (cuda_fft<<<blocks,threads>>>, :135)
  *       -> gsn_ntt on caller-owned device memory
  *   the omega powers computed per thread by Scalar::pow
- *       (cuda/device_field_operators.h:229-257, fft_kernel.cu:92-95)
+ *       (cuda/device_field_operators.h:229-257, fft_kernel.cu:65-68,90,95)
  *       -> gsn_prepare (device-resident twiddle tables)
  */
 #ifndef GPUSNARKS_GB300_H
@@ -99,19 +99,21 @@ int gsn_ntt_scratch(int field, uint32_t* data, uint32_t log_n, const uint32_t* o
 
 /* Same transform without allocating device memory (no counterpart in the
  * reference).  For callers that cannot call cudaMalloc when they run a
- * transform (inside a stream capture, in a loop that must not synchronise,
- * or with device memory owned by another allocator).  The scratch is one
- * fixed 64 MiB array inside the library, so n * limbs * 4 must not exceed
- * 64 MiB (2^24 p32, 2^21 BLS12-381, 2^19 MNT4-753 elements); only GSN_FORWARD
- * and GSN_INVERSE with the default root.  gsn_prepare(field, log_n, NULL)
- * must have run first (GSN_ERR_STATE otherwise).  The first call on a device
- * looks up the array's address, so make it before any stream capture.  All
- * calls share the array: calls that overlap on the GPU race. */
+ * transform (a loop that must not take an allocation's implicit device
+ * synchronisation, or device memory owned by another allocator).  The
+ * scratch is one fixed 64 MiB array inside the library, so n * limbs * 4
+ * must not exceed 64 MiB (2^24 p32, 2^21 BLS12-381, 2^19 MNT4-753 elements);
+ * only GSN_FORWARD and GSN_INVERSE with the default root, on the generic
+ * multi-pass kernel for every field (p32 included).
+ * gsn_prepare(field, log_n, NULL) must have run first (GSN_ERR_STATE
+ * otherwise).  The first call on a device looks up the array's address, so
+ * make it before any stream capture begins.  All calls share the array:
+ * calls that overlap on the GPU race. */
 int gsn_ntt_noalloc(int field, uint32_t* data, uint32_t log_n, int dir, void* stream);
 
 /* best_fft drop-in: `data` is host memory (pageable or pinned), transformed
  * in place; host->device copy, transform, device->host copy; returns when the
- * result is back in `data`.  Unlike cuda/fft_kernel.cu:144-174 it honours
+ * result is back in `data`.  Unlike cuda/fft_kernel.cu:117-147 it honours
  * omega, accepts any power-of-two size up to the field limit, frees what it
  * allocates and reports errors instead of exiting. */
 int gsn_ntt_host(int field, uint32_t* data, uint32_t log_n, const uint32_t* omega, int dir,
@@ -219,7 +221,7 @@ int gsn_ntt_batch(int field, const gsn_batch_job* jobs, size_t njobs, void* stre
 int gsn_batch_selftest_wait(int field, int drop_first_pass, uint32_t* status_out);
 
 /* ---- autotuning (no reference counterpart: the reference hard-codes 1024
- * chunks of 64 points, cuda/fft_kernel.cu:56-59) --------------------------- */
+ * chunks of 64 points, cuda/fft_kernel.cu:29-32,57) --------------------------- */
 
 /* Times candidate plans (pass split, tile width, threads, kernel variant)
  * for every log_n in [lo, hi] on the current device, `reps` timed runs each,
@@ -350,10 +352,10 @@ int gsn_microbench_mont(int field, int schedule, int iters, double* muls_per_s);
  * threads per element; checks 256 products against the host arithmetic
  * first (GSN_ERR_STATE on a mismatch). */
 int gsn_microbench_mont_coop(int field, int lanes, int iters, double* muls_per_s);
-/* One-limb (p32) DIF butterflies per second on the whole GPU: variant 0 the
- * compare-and-select forms, 1 the borrow-mask forms whose "+p" correction is
- * a multiply-add.  Checks that both agree element by element and match the
- * host arithmetic first (GSN_ERR_STATE on a mismatch). */
+/* One-limb (p32) DIF butterflies per second on the whole GPU, register
+ * resident, with the kernels' compare-and-select forms (variant must be 0).
+ * Checks the results against the host arithmetic first (GSN_ERR_STATE on a
+ * mismatch). */
 int gsn_microbench_p32_butterfly(int variant, int iters, double* bfly_per_s);
 
 #ifdef __cplusplus

@@ -6,13 +6,13 @@
 // `uint32_t im_rep[LIMBS]` (cuda/device_field.h:75).  The field is chosen by
 // specialising gsn::field_traits<FieldT>; the element types below come with
 // one.  Differences from the reference, all deliberate:
-//   * `omg` is used (the reference ignores it, cuda/fft_kernel.cu:144-162);
+//   * `omg` is used (the reference ignores it, cuda/fft_kernel.cu:117-147 never reads it, and the kernel uses the raw modulus limbs, :65-68);
 //     it must be a primitive a.size()-th root of unity given as a canonical
 //     integer;
 //   * any power-of-two size up to the field's limit is accepted (the
-//     reference asserts a.size() == 2^16, :150);
+//     reference asserts a.size() == 2^16, :123);
 //   * failures throw gsn::Error carrying the C ABI message instead of printing
-//     and continuing or calling exit(-1) (:61-66, :164-169);
+//     and continuing or calling exit(-1) (:34-39, :137-142);
 //   * nothing leaks (the reference never frees its two device buffers).
 #pragma once
 

@@ -139,3 +139,52 @@ def test_one_shot_ntt_batch(gsn, cuda_device):
             assert np.array_equal(gsn.to_host(t).reshape(x.shape), O.ntt(f.fid, x).reshape(x.shape))
     with pytest.raises(gsn.GsnError, match="ARG"):
         ntt_batch(f, [])
+
+
+def test_batch_at_configured_sizes(gsn, cuda_device):
+    """The batched workload at its configured sizes: 64 BLS12-381 forward jobs with log n drawn from
+    10..20 (every size present), one graph-captured persistent launch with the batched tuning table.
+    Every job equals the per-call path bit for bit; the jobs up to 2^14 also equal the oracle."""
+    import torch
+    from gpusnarks_gb300.batch import Batch, job_sizes
+    f = gsn.BLS12_381
+    sizes = list(range(10, 21)) + job_sizes(64 - 11, 10, 20, 0x5EED0404)
+    pool, views, jobs = _make_jobs(gsn, torch, f, sizes, [0] * len(sizes), 0x5EED0405)
+    small = {i: gsn.to_host(v).reshape(-1, f.limbs).copy() for i, (v, k) in enumerate(zip(views, sizes)) if k <= 14}
+    ref = [v.clone() for v in views]
+    for r in ref:
+        gsn.ntt(f, r)
+    b = Batch(f, jobs, graph=True)
+    try:
+        b.launch()
+        torch.cuda.synchronize()
+        b.status()
+    finally:
+        b.close()
+    for i, (v, r, k) in enumerate(zip(views, ref, sizes)):
+        assert torch.equal(v, r), (i, k)
+    for i, x in small.items():
+        assert np.array_equal(gsn.to_host(views[i]).reshape(x.shape), O.ntt(1, x).reshape(x.shape)), i
+
+
+def test_batch_mixed_directions_at_large_sizes_mnt4(gsn, cuda_device):
+    """MNT4-753 jobs up to 2^18 in every direction through one persistent launch, against the per-call
+    path (the batched kernel's multi-pass plans with pre/post scaling at sizes above one tile)."""
+    import torch
+    from gpusnarks_gb300.batch import Batch
+    f = gsn.MNT4_753
+    sizes = [18, 16, 14, 12, 17, 15, 13, 11]
+    dirs = [0, 1, 2, 3, 3, 2, 1, 0]
+    pool, views, jobs = _make_jobs(gsn, torch, f, sizes, dirs, 0x5EED0406)
+    ref = [v.clone() for v in views]
+    for r, d in zip(ref, dirs):
+        gsn.ntt(f, r, direction=d)
+    b = Batch(f, jobs, graph=False)
+    try:
+        b.launch()
+        torch.cuda.synchronize()
+        b.status()
+    finally:
+        b.close()
+    for v, r, k in zip(views, ref, sizes):
+        assert torch.equal(v, r), k

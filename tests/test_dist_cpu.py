@@ -67,3 +67,20 @@ def test_shard_single_rank_is_identity():
     assert shard_jobs([3, 1, 2], 1) == [[0, 1, 2]]
     with pytest.raises(ValueError):
         shard_jobs([1], 0)
+
+
+def test_mixed_field_sharding_balances_integer_work():
+    """A BLS12-381 / MNT4-753 mix balances by multiply-adds: an MNT4 transform of the same size costs
+    (2*24^2+24)/(2*8^2+8) = 8.6x a BLS one, so balancing by element count would leave one rank ~2x loaded."""
+    import numpy as np
+
+    from gpusnarks_gb300.shard import job_work, shard_jobs
+    rng = np.random.default_rng(5)
+    sizes = [int(k) for k in rng.integers(12, 23, size=400)]
+    limbs = [int(s) for s in rng.choice([8, 24], size=400)]
+    parts = shard_jobs(sizes, 2, limbs)
+    assert sorted(parts[0] + parts[1]) == list(range(400))
+    loads = [sum(job_work(sizes[i], limbs[i]) for i in p) for p in parts]
+    assert max(loads) <= 0.5 * sum(loads) * 1.02
+    with pytest.raises(ValueError):
+        shard_jobs([10, 11], 2, [8])

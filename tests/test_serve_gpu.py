@@ -203,3 +203,31 @@ def test_request_lifecycle_errors(gsn, cuda_device):
         assert np.array_equal(got, want)
     finally:
         srv.close()
+
+
+def test_serving_mix_at_configured_sizes(gsn, cuda_device):
+    """Requests at the serving workload's sizes: both fields, 2^12..2^22 (the largest of each field
+    included), forward, inverse, coset forward and coset inverse, submitted at once under a budget that
+    makes the large ones wait for memory; every result equals the plain path bit for bit."""
+    from gpusnarks_gb300.serve import Server
+    rng = np.random.default_rng(0x5EED0505)
+    reqs = []
+    for f in (gsn.BLS12_381, gsn.MNT4_753):
+        for i, k in enumerate([22, 21, 20, 18, 16, 14, 12] + [int(v) for v in rng.integers(12, 23, size=5)]):
+            d = (i + f.fid) % 4
+            x = f.device_random(1 << k, 0x5EED0500 + 100 * f.fid + i)
+            reqs.append((f, k, d, x))
+    want = [_plain(gsn, f, x, d) for f, k, d, x in reqs]
+    srv = Server(3 << 30, max_inflight=4)  # 3 GiB: an MNT4 2^22 request holds 0.8 GiB
+    try:
+        outs = [np.empty_like(x) for _, _, _, x in reqs]
+        ids = [srv.submit(f, x, d, host_out=o) for (f, k, d, x), o in zip(reqs, outs)]
+        for rid in ids:
+            srv.wait(rid, timeout_s=120.0)
+            srv.release(rid)
+        st = srv.stats()
+    finally:
+        srv.close()
+    for (f, k, d, _), o, w in zip(reqs, outs, want):
+        assert np.array_equal(o, w), (f.name, k, d)
+    assert st["failed"] == 0 and st["device_bytes_peak"] <= 3 << 30

@@ -1,6 +1,6 @@
 """gsn_ntt_noalloc: the transform for callers that cannot allocate device
-memory at call time (inside a stream capture, in loops that must not
-synchronise, or with memory owned by another allocator).  It uses a fixed
+memory at call time (loops that must not take an allocation's implicit
+device synchronisation, or memory owned by another allocator).  It uses a fixed
 scratch array compiled into the library instead of the per-stream scratch
 gsn_ntt grows with cudaMalloc.
 
