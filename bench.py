@@ -225,7 +225,15 @@ def imad_peak(g) -> dict:
     lib = g.load()
     a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
     g._lib.check(lib.gsn_microbench_imad(20000, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
-    return {"mads_per_s": a.value, "mads_per_clk_sm": b.value, "sm_mhz": c.value}
+    out = {"mads_per_s": a.value, "mads_per_clk_sm": b.value, "sm_mhz": c.value}
+    # the carry-free forms beside it: instructions per second, and per SM per clock at the same clock
+    sms = max(1, int(__import__("torch").cuda.get_device_properties(0).multi_processor_count))
+    for form, name in ((1, "mad_wide"), (2, "mad_lo"), (3, "mad_hi")):
+        v = ctypes.c_double()
+        g._lib.check(lib.gsn_microbench_imad_form(form, 20000, ctypes.byref(v)))
+        out[f"{name}_per_s"] = v.value
+        out[f"{name}_per_clk_sm"] = v.value / sms / (c.value * 1e6) if c.value > 0 else None
+    return out
 
 
 def montgomery_schedules(g, iters: int = 2000) -> dict:
@@ -350,6 +358,22 @@ def profiled_traffic(key: str):
     for ln in path.read_text().splitlines():
         if ln.startswith(key + ":"):
             return int(ln.split(":", 1)[1].split()[0])
+    return None
+
+
+def profiled_pipe(key: str):
+    """(fmaheavy-busy % per launch, durations us) recorded in profiles/traffic.txt as
+    `pipe <kernel> <size>: a b c durations_us x y z` lines; None when absent."""
+    path = ROOT / "profiles" / "traffic.txt"
+    if not path.exists():
+        return None
+    for ln in path.read_text().splitlines():
+        if ln.startswith("pipe " + key + ":"):
+            body = ln.split(":", 1)[1].split()
+            if "durations_us" in body:
+                i = body.index("durations_us")
+                return [float(v) for v in body[:i]], [float(v) for v in body[i + 1:]]
+            return [float(v) for v in body], None
     return None
 
 
@@ -481,6 +505,56 @@ def poly_product_2_21(g, torch, reps=5):
             "verified_vs_oracle": bool(np.array_equal(c, want)),
             "cpu_port": {"ms": round(t_cpu * 1e3, 1), "cores": threads, "log_cpus": log_cpus, "kind": "port",
                          "what": "three restated host FFTs of 2^21 + numpy pointwise product and n^-1 scale"}}
+
+
+def multiexp_bench(g, torch, hbm_gbs, imad_per_s, reps=10):
+    """sum_i a[i] b[i] (the reference's multiexp for field elements) per field at a size well above L2:
+    device-resident inputs, CUDA-event time of the two launches, elements/s against the HBM roofline (both
+    arrays read once: 2 x 4N bytes per element) and against the multiply-add roofline (N^2 word products
+    per element, 2 IMAD each); a 4097-element case checked against the oracle; the oracle's serial
+    restatement of test/multiexp.h (as the reference runs it) timed on a subset beside it."""
+    import oracle
+    from gpusnarks_gb300.batch import fill_random
+    out = {}
+    stream = torch.cuda.current_stream()
+    for f, log_n, cpu_n in ((g.P32, 26, 1 << 22), (g.BLS12_381, 24, 1 << 18), (g.MNT4_753, 21, 1 << 15)):
+        n = 1 << log_n
+        a = torch.empty(n * f.limbs, dtype=torch.int32, device="cuda")
+        b = torch.empty(n * f.limbs, dtype=torch.int32, device="cuda")
+        fill_random(f, a, SEED + 600 + f.fid)
+        fill_random(f, b, SEED + 700 + f.fid)
+        r = torch.empty(f.limbs, dtype=torch.int32, device="cuda")
+        for _ in range(3):
+            g.multiexp(f, a, b, r)
+        torch.cuda.synchronize()
+        ts = []
+        for _ in range(reps):
+            s0, e0 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            s0.record(stream)
+            g.multiexp(f, a, b, r)
+            e0.record(stream)
+            e0.synchronize()
+            ts.append(s0.elapsed_time(e0) * 1e-3)
+        t = float(np.median(ts))
+        del a, b
+        x = f.random_array(4097, seed=SEED + 800 + f.fid)
+        y = f.random_array(4097, seed=SEED + 900 + f.fid)
+        got = g.to_host(g.multiexp(f, g.to_device(x), g.to_device(y)))
+        verified = bool(np.array_equal(got, oracle.multiexp(f.fid, x, y)))
+        xc = f.device_random(cpu_n, SEED + 1000 + f.fid)
+        yc = f.device_random(cpu_n, SEED + 1100 + f.fid)
+        t0 = time.perf_counter()
+        oracle.multiexp(f.fid, xc, yc)
+        t_cpu = time.perf_counter() - t0
+        nbytes = 2 * 4 * f.limbs * n
+        imad = 2 * f.limbs * f.limbs * n
+        out[f.name] = {"log_n": log_n, "ms": round(t * 1e3, 4), "Gelem_s": round(n / t / 1e9, 3),
+                       "hbm_frac": round(nbytes / t / 1e9 / hbm_gbs, 4),
+                       "imad_frac": round(imad / t / imad_per_s, 4), "launches": 2,
+                       "verified_vs_oracle_4097": verified,
+                       "cpu_port": {"Melem_s": round(cpu_n / t_cpu / 1e6, 3), "elements": cpu_n, "cores": 1,
+                                    "kind": "port", "sample": "serial restatement of test/multiexp.h:3-13"}}
+    return out
 
 
 def batch_vs_per_call(g, torch, njobs=4096, lo=10, hi=20, reps=3):
@@ -619,6 +693,16 @@ def run_gpu(args, rank, local, ws):
                                 "Melem_s": round(n / PUBLISHED_REF_768_2_18_S / 1e6, 5)},
     }
     line["roofline"]["traffic"] = profiled_traffic("ntt_pass_kernel<FieldMNT4_753> 2^18")
+    # the same fraction read off the hardware: ncu's fmaheavy-pipe busy cycles of the headline passes,
+    # duration-weighted, over those of the denominator kernel (profiles/imad_pipe_*.md)
+    pp, pd = profiled_pipe("ntt_pass_kernel<FieldMNT4_753> 2^18") or (None, None), profiled_pipe("imad_chain_kernel")
+    if pp and pp[0] and pd:
+        busy = float(np.average(pp[0], weights=pp[1])) if pp[1] else float(np.mean(pp[0]))
+        line["roofline"]["pipe_check"] = {
+            "fmaheavy_busy_pct": round(busy, 2), "denominator_fmaheavy_busy_pct": pd[0][0],
+            "frac_vs_pipe": round(busy / pd[0][0], 4),
+            "source": "ncu sm__pipe_fmaheavy_cycles_active of the three passes (duration-weighted) and of "
+                      "imad_chain_kernel, profiles/imad_pipe_multiply_forms_and_pass_kernels.md"}
     if rank == 0 and ws == 1:
         line["cpu_baseline"] = cpu_baseline(args)
     if not args.headline_only and rank == 0:
@@ -630,6 +714,7 @@ def run_gpu(args, rank, local, ws):
         extra["p32_2^16"] = config1_p32_2_16(g, torch, flush, hbm_gbs)
         extra["p32_sweep"] = p32_sweep(g, torch, flush, hbm_gbs)
         extra["poly_product_2^21"] = poly_product_2_21(g, torch)
+        extra["multiexp"] = multiexp_bench(g, torch, hbm_gbs, ip["mads_per_s"])
         extra["hbm_peak_gbs"] = hbm_gbs
         try:
             extra["bls12_381_batch_4096"] = batch_vs_per_call(g, torch)

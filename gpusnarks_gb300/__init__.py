@@ -25,7 +25,8 @@ DIRECTIONS = {"forward": FORWARD, "inverse": INVERSE, "coset_forward": COSET_FOR
 __all__ = ["Field", "P32", "BLS12_381", "MNT4_753", "MNT4_753_Q", "FIELDS", "BY_ID", "GsnError",
            "FORWARD", "INVERSE", "COSET_FORWARD", "COSET_INVERSE", "load", "library_path",
            "declared_symbols", "best_fft", "ntt", "root_of_unity", "field_of", "pointwise_mul",
-           "prepare", "launch_count"]
+           "prepare", "launch_count", "multiexp", "multiexp_host", "MULTIEXP_CANONICAL",
+           "MULTIEXP_MONTGOMERY"]
 
 
 def field_of(f) -> Field:
@@ -178,6 +179,41 @@ def fft_ref_compat(data, omega_limbs, log_cpus: int = 10, *, stream=None):
     check(load().gsn_fft_ref_compat(data.data_ptr(), _log2_exact(n), u32p(w), int(log_cpus),
                                     _stream_handle(stream)))
     return data
+
+
+MULTIEXP_CANONICAL, MULTIEXP_MONTGOMERY = 0, 1
+
+
+def multiexp(field, a, b, out=None, *, mode=MULTIEXP_CANONICAL, stream=None):
+    """sum_i a[i] * b[i] mod p on the GPU (the reference's multiexp over field elements,
+    cuda/multi_exp.cu:104-137).  ``a``, ``b``: device tensors of n elements; ``out``: a device tensor of
+    one element (allocated when None).  Asynchronous on ``stream``; returns ``out``."""
+    import torch
+    f = field_of(field)
+    n = a.numel() // f.limbs
+    if b.numel() != a.numel():
+        raise ValueError("a and b must hold the same number of elements")
+    if out is None:
+        out = torch.empty(f.limbs, dtype=torch.int32, device=a.device)
+    check(load().gsn_multiexp(f.fid, a.data_ptr(), b.data_ptr(), n, out.data_ptr(), int(mode),
+                              _stream_handle(stream)))
+    return out
+
+
+def multiexp_host(a: np.ndarray, b: np.ndarray, *, field=None, mode=MULTIEXP_CANONICAL) -> np.ndarray:
+    """The same from host arrays, like the reference's multiexp(std::vector&, std::vector&): returns the
+    one result element as limbs."""
+    a = np.ascontiguousarray(a, dtype=np.uint32)
+    b = np.ascontiguousarray(b, dtype=np.uint32)
+    if field is None:
+        field = {1: P32, 8: BLS12_381, 24: MNT4_753}[1 if a.ndim == 1 else a.shape[1]]
+    f = field_of(field)
+    if a.size != b.size:
+        raise ValueError("a and b must hold the same number of elements")
+    out = np.zeros(f.limbs, dtype=np.uint32)
+    check(load().gsn_multiexp_host(f.fid, a.ctypes.data, b.ctypes.data, a.size // f.limbs, out.ctypes.data,
+                                   int(mode)))
+    return out
 
 
 TO_MONTGOMERY, FROM_MONTGOMERY, REVERSE_LIMBS = 0, 1, 2

@@ -51,6 +51,10 @@ _SIGNATURES = [
                                           ctypes.c_uint32, _u32p, ctypes.c_void_p]),
     ("gsn_qap_h", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32,
                                  _u32p, ctypes.c_void_p]),
+    ("gsn_multiexp", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_void_p,
+                                    ctypes.c_int, ctypes.c_void_p]),
+    ("gsn_multiexp_host", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint64,
+                                         ctypes.c_void_p, ctypes.c_int]),
     ("gsn_fft_ref_compat", ctypes.c_int, [ctypes.c_void_p, ctypes.c_uint32, _u32p, ctypes.c_int, ctypes.c_void_p]),
     ("gsn_convert", ctypes.c_int, [ctypes.c_int, ctypes.c_void_p, ctypes.c_uint64, ctypes.c_int, ctypes.c_void_p]),
     ("gsn_synchronize", ctypes.c_int, [ctypes.c_void_p]),
@@ -60,6 +64,7 @@ _SIGNATURES = [
     ("gsn_kernel_launch_count", ctypes.c_uint64, []),
     ("gsn_microbench_imad", ctypes.c_int, [ctypes.c_int, ctypes.POINTER(ctypes.c_double),
                                            ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]),
+    ("gsn_microbench_imad_form", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_double)]),
     ("gsn_microbench_mont", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.POINTER(ctypes.c_double)]),
     ("gsn_microbench_mont_coop", ctypes.c_int, [ctypes.c_int, ctypes.c_int, ctypes.c_int,

@@ -58,6 +58,25 @@ std::vector<Plan> candidates(const FieldOps& F, int log_n) {
           }
       }
   }
+  if (F.id == GSN_BLS12_381_FR) {
+    // register-blocked passes: one to three passes of radix <= 2^10, sub-steps of 4 or 8 rows, 2 or 4 columns
+    auto rb = [&](const int* radix, int np) {
+      for (int lj = 1; lj <= 2; ++lj)
+        for (int e = 2; e <= 3; ++e) add(make_rb_plan(F, log_n, radix, np, lj, e));
+    };
+    if (log_n <= 10) {
+      const int one[1] = {log_n};
+      rb(one, 1);
+    }
+    for (int a = 2; a <= 10; ++a) {
+      const int two[2] = {a, log_n - a};
+      if (log_n - a >= 2 && log_n - a <= 10) rb(two, 2);
+      for (int b = 2; b <= 10; ++b) {
+        const int three[3] = {a, b, log_n - a - b};
+        if (three[2] >= 2 && three[2] <= 10 && log_n > 20) rb(three, 3);
+      }
+    }
+  }
   if (F.id == GSN_P32 && log_n >= 8) {
     for (int max_r = 7; max_r <= 14; ++max_r)
       for (int lj = 2; lj <= 3; ++lj)

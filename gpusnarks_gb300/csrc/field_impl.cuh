@@ -5,7 +5,9 @@
 
 #include "field_ops.h"
 #include "host_field.h"
+#include "multiexp.cuh"
 #include "ntt_kernels.cuh"
+#include "ntt_rb.cuh"
 
 namespace gsn {
 
@@ -45,6 +47,7 @@ constexpr FieldOps make_field_ops(int max_log_n, int default_tw_log) {
                   default_tw_log,
                   P::GENERATOR,
                   &Kernels<P>::pass,
+                  &RbKernels<P>::pass,
                   &Kernels<P>::powers,
                   &Kernels<P>::pointwise,
                   &Kernels<P>::quotient,
@@ -52,6 +55,8 @@ constexpr FieldOps make_field_ops(int max_log_n, int default_tw_log) {
                   &Kernels<P>::convert,
                   &Kernels<P>::batch,
                   &Kernels<P>::batch_occupancy,
+                  &MultiexpKernels<P>::grid,
+                  &MultiexpKernels<P>::run,
                   &HostOps<P>::root,
                   &HostOps<P>::is_primitive,
                   &HostOps<P>::is_canonical,

@@ -77,6 +77,82 @@ __global__ void imad_chain_kernel(uint32_t* sink, int iters, uint32_t x, uint32_
   }
 }
 
+// The multiply-add forms without a carry flag, for comparison with the carry chains above: every thread
+// runs kFormChains independent accumulators, each step one PTX instruction per accumulator.
+//   form 1: mad.wide.u32  acc64 += a * b     (one 32x32->64 word product per instruction)
+//   form 2: mad.lo.u32    acc32 += lo(a * b)
+//   form 3: mad.hi.u32    acc32 += hi(a * b)
+// The multiplier a changes every step so no product is loop-invariant.
+constexpr int kFormChains = 8;
+
+template <int FORM>
+__global__ void imad_form_kernel(uint32_t* sink, int iters, uint32_t x, uint32_t y) {
+  uint32_t u = x ^ threadIdx.x;
+  uint32_t v[kFormChains];
+#pragma unroll
+  for (int c = 0; c < kFormChains; ++c) v[c] = y + blockIdx.x + 977u * c;
+  if constexpr (FORM == 1) {
+    uint64_t acc[kFormChains];
+#pragma unroll
+    for (int c = 0; c < kFormChains; ++c) acc[c] = threadIdx.x * (c + 1);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+      for (int c = 0; c < kFormChains; ++c) asm volatile("mad.wide.u32 %0, %1, %2, %0;" : "+l"(acc[c]) : "r"(u), "r"(v[c]));
+      u += 0x9E3779B9u;
+    }
+    uint64_t t = 0;
+#pragma unroll
+    for (int c = 0; c < kFormChains; ++c) t ^= acc[c];
+    if (t == 0x123456789ull) sink[threadIdx.x] = (uint32_t)t;
+  } else {
+    uint32_t acc[kFormChains];
+#pragma unroll
+    for (int c = 0; c < kFormChains; ++c) acc[c] = threadIdx.x * (c + 1);
+    for (int it = 0; it < iters; ++it) {
+#pragma unroll
+      for (int c = 0; c < kFormChains; ++c) {
+        if constexpr (FORM == 2) asm volatile("mad.lo.u32 %0, %1, %2, %0;" : "+r"(acc[c]) : "r"(u), "r"(v[c]));
+        else asm volatile("mad.hi.u32 %0, %1, %2, %0;" : "+r"(acc[c]) : "r"(u), "r"(v[c]));
+      }
+      u += 0x9E3779B9u;
+    }
+    uint32_t t = 0;
+#pragma unroll
+    for (int c = 0; c < kFormChains; ++c) t ^= acc[c];
+    if (t == 0x12345678u) sink[threadIdx.x] = t;
+  }
+}
+
+template <int FORM>
+static int run_imad_form(int iters, double* ops_per_s) {
+  int dev = 0, sms = 0, per_sm = 0;
+  GSN_CUDA(cudaGetDevice(&dev));
+  GSN_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int block = 256;
+  GSN_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, imad_form_kernel<FORM>, block, 0));
+  const int grid = sms * std::max(per_sm, 1);
+  uint32_t* sink = nullptr;
+  int rc = dev_alloc((void**)&sink, block * sizeof(uint32_t));
+  if (rc) return rc;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  imad_form_kernel<FORM><<<grid, block>>>(sink, iters / 8 + 1, 3u, 5u);
+  cudaEventRecord(e0);
+  imad_form_kernel<FORM><<<grid, block>>>(sink, iters, 3u, 5u);
+  cudaEventRecord(e1);
+  cudaError_t err = cudaEventSynchronize(e1);
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  dev_free(sink);
+  count_launches(2);
+  if (err != cudaSuccess) return cuda_fail(err, "multiply-add form microbenchmark");
+  *ops_per_s = (double)grid * block * iters * kFormChains / (ms * 1e-3);
+  return GSN_OK;
+}
+
 // Throughput of the field Montgomery product itself: every thread runs two
 // independent chains x <- x * y.  S selects the multi-limb schedule.
 template <class P, int S>
@@ -536,6 +612,16 @@ extern "C" int gsn_microbench_mont(int field, int schedule, int iters, double* m
     case GSN_MNT4753_FR * 3 + 1: return run_mont_bench<FieldMNT4_753, 1>(iters, muls_per_s);
     case GSN_MNT4753_FR * 3 + 2: return run_mont_bench<FieldMNT4_753, 2>(iters, muls_per_s);
     default: return set_error(GSN_ERR_FIELD, "Montgomery microbenchmark covers the multi-limb fields");
+  }
+}
+
+extern "C" int gsn_microbench_imad_form(int form, int iters, double* ops_per_s) {
+  if (iters <= 0 || !ops_per_s) return set_error(GSN_ERR_ARG, "bad microbenchmark arguments");
+  switch (form) {
+    case 1: return run_imad_form<1>(iters, ops_per_s);
+    case 2: return run_imad_form<2>(iters, ops_per_s);
+    case 3: return run_imad_form<3>(iters, ops_per_s);
+    default: return set_error(GSN_ERR_ARG, "form must be 1 (mad.wide), 2 (mad.lo) or 3 (mad.hi)");
   }
 }
 

@@ -124,6 +124,11 @@ bool plan_valid(const FieldOps& F, const Plan& p) {
     if (F.id != GSN_P32 || p.npass < 2 || (p.e_log != 3 && p.e_log != 4)) return false;
     for (int i = 0; i < p.npass; ++i)
       if (p.log_j[i] < 2 || p.log_j[i] > 4 || p.radix_log[i] < 2 || p.block[i] > 512) return false;
+  } else if (p.kernel == kKernelRB) {
+    // 16-byte limb planes, at most 4 columns per tile (the swizzle), sub-steps of 4 or 8 rows
+    if (F.id != GSN_BLS12_381_FR || (p.e_log != 2 && p.e_log != 3)) return false;
+    for (int i = 0; i < p.npass; ++i)
+      if (p.log_j[i] > 2 || p.radix_log[i] < 1 || p.block[i] > 256) return false;
   } else if (p.kernel != kKernelGeneric) {
     return false;
   }
@@ -227,6 +232,17 @@ Plan make_p32_plan(int log_n, int max_r, int log_j, int e_log) {
   return p;
 }
 
+Plan make_rb_plan(const FieldOps& F, int log_n, const int* radix_log, int npass, int log_j, int e_log) {
+  Plan p = make_split_plan(F, log_n, radix_log, npass, log_j, 256);
+  p.kernel = kKernelRB;
+  p.e_log = e_log;
+  for (int i = 0; i < p.npass; ++i) {
+    const int elems = 1 << (p.radix_log[i] + p.log_j[i]);
+    p.block[i] = std::max(32, std::min(256, elems >> std::min(e_log, p.radix_log[i])));
+  }
+  return p;
+}
+
 Plan plan_for(const FieldOps& F, int log_n, bool batched) {
   Plan p;
   // batched plans come from their own table: a persistent launch runs every
@@ -235,6 +251,14 @@ Plan plan_for(const FieldOps& F, int log_n, bool batched) {
   const int mode = batched ? 1 : 0;
   if (get_tuned_plan(F.id, log_n, &p, mode) && plan_valid(F, p) && (!batched || p.kernel == kKernelGeneric))
     return p;
+  if (F.id == GSN_BLS12_381_FR && !batched && log_n >= 2) {
+    // register-blocked passes of radix <= 2^10 over 4-column tiles
+    const int npass = std::max(1, (log_n + 9) / 10);
+    int radix[kMaxPasses] = {0, 0, 0, 0};
+    for (int i = 0; i < npass; ++i) radix[i] = log_n / npass + (i < log_n % npass ? 1 : 0);
+    p = make_rb_plan(F, log_n, radix, npass, 2, 3);
+    if (plan_valid(F, p)) return p;
+  }
   if (F.id == GSN_P32 && !batched && log_n >= 8) {
     // tiles of at most 2^14 elements (64 KB): J = 8 columns, radix <= 2^11
     p = make_p32_plan(log_n, 11, 3, 4);
@@ -483,6 +507,7 @@ static int enqueue_p32(const Plan& plan, const Tables& T, uint32_t* data, uint32
 int enqueue_ntt(const FieldOps& F, const Plan& plan, const Tables& T, uint32_t* data, uint32_t* scratch,
                 cudaStream_t s) {
   if (plan.kernel == kKernelP32) return enqueue_p32(plan, T, data, scratch, s);
+  const bool rb = plan.kernel == kKernelRB;
   PassArgs A;
   std::memset(&A, 0, sizeof(A));
   A.tw = T.tw;
@@ -506,7 +531,7 @@ int enqueue_ntt(const FieldOps& F, const Plan& plan, const Tables& T, uint32_t* 
     A.post_table = A.last ? T.post_table : nullptr;
     A.has_pre_const = A.first ? T.has_pre_const : 0;
     if (A.has_pre_const) std::memcpy(A.pre_const, T.pre_const, sizeof(A.pre_const));
-    cudaError_t e = F.pass(A, plan.block[p], s);
+    cudaError_t e = rb ? F.pass_rb(A, plan.e_log, plan.block[p], s) : F.pass(A, plan.block[p], s);
     if (e != cudaSuccess) return cuda_fail(e, "NTT pass launch");
     count_launches(1);
     outer += plan.radix_log[p];
@@ -800,6 +825,99 @@ int gsn_ntt_host_batch(int field, uint32_t* const* data, size_t count, uint32_t 
   host_state_release(h);
   return rc;
 }
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// multi-exponentiation over field elements (cuda/multi_exp.cu:104-137, test/multiexp.h:3-13)
+// ---------------------------------------------------------------------------
+namespace gsn {
+// The representation constant of multiexp.cuh: 2^(32(2N+1)) mod p (canonical) or 2^(32(N+1)) mod p
+// (Montgomery), canonical limbs.
+static void multiexp_fix(const FieldOps& F, int mode, uint32_t* fix) {
+  uint32_t two[kMaxLimbs] = {0};
+  two[0] = 2;
+  const int N = F.limbs;
+  F.pow(two, (uint64_t)32 * (mode == GSN_MULTIEXP_CANONICAL ? 2 * N + 1 : N + 1), fix);
+}
+
+static int multiexp_impl(const FieldOps& F, const uint32_t* a, const uint32_t* b, uint64_t n, uint32_t* out,
+                         int mode, cudaStream_t s) {
+  const int grid = F.multiexp_grid(n);
+  uint32_t* partial = nullptr;
+  int rc = scratch_for(s, (size_t)grid * F.limbs * sizeof(uint32_t), &partial);
+  if (rc) return rc;
+  uint32_t fix[kMaxLimbs];
+  multiexp_fix(F, mode, fix);
+  cudaError_t e = F.multiexp(a, b, n, partial, grid, out, fix, s);
+  if (e != cudaSuccess) return cuda_fail(e, "multiexp launch");
+  count_launches(2);
+  return GSN_OK;
+}
+
+// Arguments shared by the device and host entry points.
+static int multiexp_check(const FieldOps* F, int field, const void* a, const void* b, uint64_t n, const void* out,
+                          int mode) {
+  if (!F) return set_error(GSN_ERR_FIELD, "unknown field %d", field);
+  if (mode != GSN_MULTIEXP_CANONICAL && mode != GSN_MULTIEXP_MONTGOMERY)
+    return set_error(GSN_ERR_ARG, "bad multiexp mode %d", mode);
+  if (!out) return set_error(GSN_ERR_ARG, "null output");
+  if (n && (!a || !b)) return set_error(GSN_ERR_ARG, "null input array");
+  // every thread's integer accumulator stays below p * 2^(32(N+1)) while it adds fewer than 2^32 products
+  if (n > ((uint64_t)1 << 40)) return set_error(GSN_ERR_SIZE, "n = %llu exceeds 2^40", (unsigned long long)n);
+  return GSN_OK;
+}
+}  // namespace gsn
+
+extern "C" {
+
+int gsn_multiexp(int field, const uint32_t* a, const uint32_t* b, uint64_t n, uint32_t* out, int mode,
+                 void* stream) {
+  const FieldOps* F = field_ops(field);
+  int rc = multiexp_check(F, field, a, b, n, out, mode);
+  if (rc) return rc;
+  const uintptr_t align = (F->limbs % 4 == 0) ? 16 : 4;
+  if ((reinterpret_cast<uintptr_t>(out) % align) ||
+      (n && ((reinterpret_cast<uintptr_t>(a) % align) || (reinterpret_cast<uintptr_t>(b) % align))))
+    return set_error(GSN_ERR_ARG, "a, b and out must be %zu-byte aligned", (size_t)align);
+  return multiexp_impl(*F, a, b, n, out, mode, static_cast<cudaStream_t>(stream));
+}
+
+int gsn_multiexp_host(int field, const uint32_t* a, const uint32_t* b, uint64_t n, uint32_t* out, int mode) {
+  const FieldOps* F = field_ops(field);
+  int rc = multiexp_check(F, field, a, b, n, out, mode);
+  if (rc) return rc;
+  HostState* h = nullptr;
+  rc = host_state_acquire(&h);
+  if (rc) return rc;
+  const size_t bytes = (size_t)n * F->limbs * sizeof(uint32_t), rbytes = F->limbs * sizeof(uint32_t);
+  rc = host_state_buffer(h, 0, bytes);
+  if (!rc) rc = host_state_buffer(h, 1, bytes);
+  if (!rc) rc = host_state_buffer(h, 2, rbytes);
+  if (!rc) {
+    const cudaStream_t s = h->s_comp;
+    uint32_t* da = static_cast<uint32_t*>(h->bufs[0].p);
+    uint32_t* db = static_cast<uint32_t*>(h->bufs[1].p);
+    uint32_t* dout = static_cast<uint32_t*>(h->bufs[2].p);
+    cudaError_t e = cudaSuccess;
+    if (bytes) e = cudaMemcpyAsync(da, a, bytes, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(db, b, bytes, cudaMemcpyHostToDevice, s);
+    if (e != cudaSuccess) rc = cuda_fail(e, "host-to-device copy");
+    if (!rc) rc = multiexp_impl(*F, da, db, n, dout, mode, s);
+    if (!rc) {
+      e = cudaMemcpyAsync(out, dout, rbytes, cudaMemcpyDeviceToHost, s);
+      if (e != cudaSuccess) rc = cuda_fail(e, "device-to-host copy");
+    }
+    e = cudaStreamSynchronize(s);
+    if (!rc && e != cudaSuccess) rc = cuda_fail(e, "cudaStreamSynchronize");
+  }
+  host_state_release(h);
+  return rc;
+}
+
+}  // extern "C"
+
+extern "C" {
 
 int gsn_prepare(int field, uint32_t log_n, const uint32_t* omega) {
   const FieldOps* F = field_ops(field);

@@ -28,7 +28,7 @@ void count_launches(uint64_t n);
 
 // A transform plan: pass split, tile shape and threads per pass, and which
 // kernel runs the passes.
-enum PlanKernel { kKernelGeneric = 0, kKernelP32 = 1 };
+enum PlanKernel { kKernelGeneric = 0, kKernelP32 = 1, kKernelRB = 2 };
 
 struct Plan {
   int log_n = 0;
@@ -36,8 +36,9 @@ struct Plan {
   int radix_log[kMaxPasses] = {0, 0, 0, 0};
   int log_j[kMaxPasses] = {0, 0, 0, 0};
   int block[kMaxPasses] = {0, 0, 0, 0};
-  int kernel = kKernelGeneric;  // kKernelP32: register-blocked 32-bit pass (ntt_p32.cuh)
-  int e_log = 4;                // kKernelP32: rows per thread per register sub-step (log2)
+  int kernel = kKernelGeneric;  // kKernelP32: register-blocked 32-bit pass (ntt_p32.cuh);
+                                // kKernelRB: register-blocked multi-limb pass (ntt_rb.cuh)
+  int e_log = 4;                // kKernelP32 / kKernelRB: rows per thread per register sub-step (log2)
 };
 
 // Register-blocked 32-bit pass launcher (ntt_f_p32.cu).
@@ -47,6 +48,9 @@ cudaError_t launch_p32_pass(const P32Args& A, int e_log, int block, int grid_cap
 // loaded.
 Plan plan_for(const FieldOps& F, int log_n, bool batched = false);
 Plan make_p32_plan(int log_n, int max_r, int log_j, int e_log);
+// Register-blocked multi-limb plan over an explicit radix split: 2^log_j columns per tile (<= 4), 2^e_log
+// rows per thread per sub-step.
+Plan make_rb_plan(const FieldOps& F, int log_n, const int* radix_log, int npass, int log_j, int e_log);
 // Heuristic plan with explicit limits (used by the autotuner's candidate set).
 Plan make_plan(const FieldOps& F, int log_n, int max_r, int target_j, int max_block);
 // The same tile widths and threads for an explicit split of log_n into npass radices.

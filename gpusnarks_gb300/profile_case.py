@@ -2,6 +2,7 @@
 
     python -m gpusnarks_gb300.profile_case --field p32 --log-n 24 --reps 3
     python -m gpusnarks_gb300.profile_case --field bls12_381_fr --batch 512 --batch-lo 10 --batch-hi 18
+    python -m gpusnarks_gb300.profile_case --microbench imad --iters 2000
 
 Fills the input on the device (gsn_fill_random), runs `warmup` untimed and
 `reps` further transforms through the C ABI, prints the mean event time.
@@ -24,6 +25,9 @@ def main() -> None:
     ap.add_argument("--batch", type=int, default=0, help="jobs in one batched launch (0: one transform)")
     ap.add_argument("--batch-lo", type=int, default=10)
     ap.add_argument("--batch-hi", type=int, default=18)
+    ap.add_argument("--microbench", default="", choices=["", "imad", "imad_wide", "imad_lo", "imad_hi"],
+                    help="run one integer multiply-add microbenchmark instead (--iters steps per thread)")
+    ap.add_argument("--iters", type=int, default=2000)
     args = ap.parse_args()
 
     import torch
@@ -31,6 +35,9 @@ def main() -> None:
     import gpusnarks_gb300 as g
     from gpusnarks_gb300.batch import fill_random
 
+    if args.microbench:
+        run_microbench(g, args)
+        return
     f = g.FIELDS[args.field]
     if args.batch:
         run_batch(g, torch, f, args)
@@ -50,6 +57,22 @@ def main() -> None:
     ms = s.elapsed_time(e) / max(args.reps, 1)
     print(f"{args.field} 2^{args.log_n}: {ms:.4f} ms per transform, {n / ms / 1e3:.1f} Melem/s")
 
+
+
+def run_microbench(g, args) -> None:
+    """gsn_microbench_imad (carry chains: a warm-up launch, then the timed one) or one carry-free form of
+    gsn_microbench_imad_form (the same two launches)."""
+    import ctypes
+    lib = g.load()
+    if args.microbench == "imad":
+        a, b, c = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        g._lib.check(lib.gsn_microbench_imad(args.iters, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        print(f"carry-chain multiply-adds: {a.value / 1e12:.3f} T/s, {b.value:.1f} per SM per clock at {c.value:.0f} MHz")
+        return
+    form = {"imad_wide": 1, "imad_lo": 2, "imad_hi": 3}[args.microbench]
+    v = ctypes.c_double()
+    g._lib.check(lib.gsn_microbench_imad_form(form, args.iters, ctypes.byref(v)))
+    print(f"{args.microbench}: {v.value / 1e12:.3f} T instructions/s")
 
 
 def run_batch(g, torch, f, args) -> None:

@@ -156,6 +156,26 @@ int gsn_coset_quotient(int field, uint32_t* a, const uint32_t* b, const uint32_t
 int gsn_qap_h(int field, uint32_t* a, uint32_t* b, uint32_t* c, uint32_t log_n, const uint32_t* shift,
               void* stream);
 
+/* Multi-exponentiation over field elements: *out = sum_{i<n} a[i] * b[i]
+ * mod p.  Replaces multiexp<FieldT, FieldMul>(std::vector<FieldT>&,
+ * std::vector<FieldMul>&) (cuda/multi_exp.h:24-25, cuda/multi_exp.cu:104-137)
+ * for field elements; its CPU counterpart is multi_exp (test/multiexp.h:3-13).
+ *   GSN_MULTIEXP_CANONICAL   a, b and *out are canonical integers;
+ *   GSN_MULTIEXP_MONTGOMERY  a, b are Montgomery forms xR, yR and *out is
+ *                            (sum x y) R: each term is the Montgomery product
+ *                            of the stored words, as the reference's
+ *                            Scalar::operator* is (device_field.h:115-122).
+ * Device pointers (16-byte aligned for the 8- and 24-limb fields), n may be
+ * 0 (*out = 0); two launches on `stream`, asynchronous.  The elliptic-curve
+ * instantiations of the reference (fp2, mnt4753_G1, multi_exp.cu:141-142)
+ * are not provided. */
+enum { GSN_MULTIEXP_CANONICAL = 0, GSN_MULTIEXP_MONTGOMERY = 1 };
+int gsn_multiexp(int field, const uint32_t* a, const uint32_t* b, uint64_t n, uint32_t* out, int mode,
+                 void* stream);
+/* Same from host memory, like the reference's multiexp: copies a and b in,
+ * computes, copies the one result element back, returns when *out is set. */
+int gsn_multiexp_host(int field, const uint32_t* a, const uint32_t* b, uint64_t n, uint32_t* out, int mode);
+
 /* Reference-compatible transform: the reference's host FFT
  * _basic_parallel_radix2_FFT_inner(a, omega, log_cpus) (test/fft_host.h:56-118)
  * run on the GPU with the reference's own fields::Scalar arithmetic and
@@ -343,6 +363,12 @@ uint64_t gsn_kernel_launch_count(void);
  * Montgomery products use, on every SM at full occupancy.  Returns PTX
  * multiply-adds per second, per SM per clock, and the SM clock seen. */
 int gsn_microbench_imad(int iters, double* mads_per_s, double* mads_per_clk_sm, double* sm_mhz);
+/* The multiply-add forms without the carry flag, on every SM at full
+ * occupancy, independent accumulators per thread (no reference counterpart):
+ * form 1 mad.wide.u32 (32x32->64 accumulate), 2 mad.lo.u32, 3 mad.hi.u32.
+ * Returns PTX instructions per second; compares the carry-chain rate of
+ * gsn_microbench_imad with what the multiply pipe issues without carries. */
+int gsn_microbench_imad_form(int form, int iters, double* ops_per_s);
 /* Throughput (products per second, all SMs) of the multi-limb Montgomery
  * product with schedule 0 (row chains), 1 (even/odd accumulators merged every
  * row) or 2 (split accumulators, carried merge); first checks 256 products of

@@ -58,6 +58,7 @@ def lib():
         _lib.oracle_arith.argtypes = [ctypes.c_int, ctypes.c_int, _u32p, _u32p, ctypes.c_uint64, _u32p]
         _lib.oracle_refscalar_arith.argtypes = [ctypes.c_int, _u32p, _u32p, ctypes.c_uint64, _u32p]
         _lib.oracle_refscalar_fft.argtypes = [_u32p, ctypes.c_int, _u32p, ctypes.c_int, ctypes.c_int]
+        _lib.oracle_multiexp.argtypes = [ctypes.c_int, _u32p, _u32p, ctypes.c_uint64, ctypes.c_int, _u32p]
     return _lib
 
 
@@ -73,6 +74,8 @@ def ref():
         _ref.ref_scalar_fft.argtypes = [_u32p, ctypes.c_int, _u32p, ctypes.c_int, ctypes.c_int]
         _ref.ref_fft_oracle_field.argtypes = [ctypes.c_int, _u32p, ctypes.c_int, _u32p, ctypes.c_int,
                                               ctypes.c_int, ctypes.c_int]
+        _ref.ref_multi_exp_oracle_field.argtypes = [ctypes.c_int, _u32p, _u32p, ctypes.c_uint64, ctypes.c_int,
+                                                    _u32p]
     return _ref
 
 
@@ -199,6 +202,34 @@ def refscalar_fft(data: np.ndarray, omega_limbs: np.ndarray, log_cpus: int, nthr
     w = np.ascontiguousarray(omega_limbs, dtype=np.uint32)
     lib().oracle_refscalar_fft(_ptr(a), n.bit_length() - 1, _ptr(w), log_cpus, nthreads)
     return a
+
+
+MULTIEXP_CANONICAL, MULTIEXP_MONTGOMERY = 0, 1
+
+
+def multiexp(fid: int, a: np.ndarray, b: np.ndarray, mode: int = MULTIEXP_CANONICAL) -> np.ndarray:
+    """sum_i a[i] * b[i], the restated multi_exp of test/multiexp.h:3-13 (serial, index order).  mode 0:
+    canonical integers in and out; mode 1: the words are Montgomery forms (each term is the Montgomery
+    product of the stored words, as the reference's Scalar::operator* is)."""
+    a = np.ascontiguousarray(a, dtype=np.uint32)
+    b = np.ascontiguousarray(b, dtype=np.uint32)
+    n = a.size // LIMBS[fid]
+    assert b.size == a.size
+    out = np.zeros(LIMBS[fid], dtype=np.uint32)
+    rc = lib().oracle_multiexp(fid, _ptr(a), _ptr(b), n, mode, _ptr(out))
+    if rc != 0:
+        raise RuntimeError(f"oracle_multiexp failed rc={rc}")
+    return out
+
+
+def multiexp_definition(fid: int, a, b, mode: int = MULTIEXP_CANONICAL) -> int:
+    """The mathematical definition with Python integers: sum a_i b_i mod p (canonical), or
+    sum a_i b_i R^-1 mod p (Montgomery forms, R = 2^(32 limbs))."""
+    p = MODULI[fid]
+    s = sum(x * y for x, y in zip(ints(fid, a), ints(fid, b))) % p
+    if mode == MULTIEXP_MONTGOMERY:
+        s = s * pow(1 << (32 * LIMBS[fid]), p - 2, p) % p
+    return s
 
 
 def max_threads() -> int:

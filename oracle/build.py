@@ -54,6 +54,7 @@ def build_ref(force: bool = False) -> pathlib.Path | None:
     REF_DIR.mkdir(exist_ok=True)
     srcs = [HERE / "ref_driver.cpp", HERE / "oracle_field.h",
             REFERENCE_ROOT / "test" / "fft_host.h",
+            REFERENCE_ROOT / "test" / "multiexp.h",
             REFERENCE_ROOT / "cuda" / "device_field.h",
             REFERENCE_ROOT / "cuda" / "device_field_operators.h"]
     if force or _stale(REF_SO, srcs):

@@ -321,6 +321,36 @@ struct RefScalar {
 
 using oracle::refscalar::RefScalar;
 
+namespace oracle {
+
+// test/multiexp.h:3-13 restated over the correct field type: result starts at zero and accumulates
+// result = result + a[i] * b[i] in index order, where * is the Montgomery product of the stored forms
+// (the reference's Scalar::operator*, cuda/device_field.h:115-122).  mode 0: a, b and the result are
+// canonical integers (entered into / taken out of Montgomery form around the loop); mode 1: the words
+// are the stored Montgomery forms themselves.
+template <int N, int FID>
+int run_multiexp(const uint32_t* a, const uint32_t* b, uint64_t n, int mode, uint32_t* out) {
+  using F = Fe<N, FID>;
+  modulus_of<N>(FID);
+  F result = F::zero();
+  for (uint64_t i = 0; i < n; ++i) {
+    F x, y;
+    if (mode == 0) {
+      x = F::from_canonical(a + i * N);
+      y = F::from_canonical(b + i * N);
+    } else {
+      std::memcpy(x.im_rep, a + i * N, sizeof(x.im_rep));
+      std::memcpy(y.im_rep, b + i * N, sizeof(y.im_rep));
+    }
+    result = result + (x * y);
+  }
+  if (mode == 0) result.to_canonical(out);
+  else std::memcpy(out, result.im_rep, sizeof(result.im_rep));
+  return 0;
+}
+
+}  // namespace oracle
+
 extern "C" {
 
 // In-place NTT of n = 2^log_n canonical elements (limbs little-endian,
@@ -378,6 +408,17 @@ int oracle_refscalar_fft(uint32_t* data, int log_n, const uint32_t* omega, int l
   parallel_fft<RefScalar, RefButterfly>(a, w, (size_t)log_cpus, RefScalar::one());
   for (size_t i = 0; i < n; ++i) std::memcpy(data + i * 24, a[i].im_rep, 96);
   return 0;
+}
+
+// sum_i a[i] * b[i] (test/multiexp.h:3-13); mode 0 canonical, 1 Montgomery forms (see run_multiexp).
+int oracle_multiexp(int field, const uint32_t* a, const uint32_t* b, uint64_t n, int mode, uint32_t* out) {
+  using namespace oracle;
+  switch (field) {
+    case F_P32: return run_multiexp<1, F_P32>(a, b, n, mode, out);
+    case F_BLS: return run_multiexp<8, F_BLS>(a, b, n, mode, out);
+    case F_MNT4R: return run_multiexp<24, F_MNT4R>(a, b, n, mode, out);
+    default: return -1;
+  }
 }
 
 int oracle_max_threads(void) { return omp_get_max_threads(); }

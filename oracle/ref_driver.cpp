@@ -13,7 +13,9 @@
 //     calls it;
 //   * the reference host FFT (unmodified, so with its own butterfly) over the
 //     oracle's correct field type oracle::Fe, which pins the loop structure of
-//     the restatement independently of the arithmetic.
+//     the restatement independently of the arithmetic;
+//   * the reference's CPU multi-exponentiation multi_exp (test/multiexp.h)
+//     over oracle::Fe, which pins the oracle's restatement of it.
 #include <omp.h>
 
 #include <cstring>
@@ -24,6 +26,7 @@
 #include "cuda/device_field.h"
 #include "cuda/device_field_operators.h"
 #include "test/fft_host.h"
+#include "test/multiexp.h"
 
 namespace {
 
@@ -38,6 +41,27 @@ int fft_over_oracle_field(uint32_t* data, int log_n, const uint32_t* omega, int 
   if (serial) _basic_serial_radix2_FFT<F>(a, w, F::one());
   else _basic_parallel_radix2_FFT_inner<F>(a, w, (size_t)log_cpus, F::one());
   for (size_t i = 0; i < n; ++i) a[i].to_canonical(data + i * N);
+  return 0;
+}
+
+// mode 0: canonical integers in and out; mode 1: the words are the stored (Montgomery) forms.
+template <int N, int FID>
+int multi_exp_over_oracle_field(const uint32_t* a, const uint32_t* b, uint64_t n, int mode, uint32_t* out) {
+  using F = oracle::Fe<N, FID>;
+  oracle::modulus_of<N>(FID);
+  std::vector<F> va(n), vb(n);
+  for (uint64_t i = 0; i < n; ++i) {
+    if (mode == 0) {
+      va[i] = F::from_canonical(a + i * N);
+      vb[i] = F::from_canonical(b + i * N);
+    } else {
+      std::memcpy(va[i].im_rep, a + i * N, sizeof(va[i].im_rep));
+      std::memcpy(vb[i].im_rep, b + i * N, sizeof(vb[i].im_rep));
+    }
+  }
+  F r = multi_exp<F, F>(va, vb);
+  if (mode == 0) r.to_canonical(out);
+  else std::memcpy(out, r.im_rep, sizeof(r.im_rep));
   return 0;
 }
 
@@ -78,6 +102,16 @@ int ref_fft_oracle_field(int field, uint32_t* data, int log_n, const uint32_t* o
       return fft_over_oracle_field<24, oracle::F_MNT4R>(data, log_n, omega, log_cpus, serial);
     case oracle::F_MNT4Q:
       return fft_over_oracle_field<24, oracle::F_MNT4Q>(data, log_n, omega, log_cpus, serial);
+    default: return -1;
+  }
+}
+
+int ref_multi_exp_oracle_field(int field, const uint32_t* a, const uint32_t* b, uint64_t n, int mode,
+                               uint32_t* out) {
+  switch (field) {
+    case oracle::F_P32: return multi_exp_over_oracle_field<1, oracle::F_P32>(a, b, n, mode, out);
+    case oracle::F_BLS: return multi_exp_over_oracle_field<8, oracle::F_BLS>(a, b, n, mode, out);
+    case oracle::F_MNT4R: return multi_exp_over_oracle_field<24, oracle::F_MNT4R>(a, b, n, mode, out);
     default: return -1;
   }
 }

@@ -18,6 +18,10 @@ Fixtures (all numpy .npz, little-endian uint32 limbs):
 * ``ref_butterfly_<field>.npz``  the reference host FFT (test/fft_host.h, its
   own butterfly) over the oracle's correct field type, on seeded inputs, both
   the serial loop and the num_cpus decomposition with log_cpus = 2.
+* ``ref_multiexp_<field>.npz``  the reference's CPU multi-exponentiation
+  multi_exp (test/multiexp.h:3-13) over the oracle's correct field type on
+  seeded vectors of several lengths (0, 1, 257, 1024), canonical integers and
+  stored Montgomery forms.  ``--only multiexp`` writes just these.
 
 Run: ``python tests/golden/make_golden.py`` (about a minute, mostly the
 2^16 reference run).
@@ -50,10 +54,37 @@ def _seeded_elements(fid: int, n: int, seed: int) -> np.ndarray:
     return oracle.array(fid, [rnd.randrange(p) for _ in range(n)])
 
 
+MULTIEXP_LENGTHS = (0, 1, 257, 1024)
+
+
+def write_multiexp(ref) -> None:
+    p_ = oracle._ptr
+    for fid in (0, 1, 2):
+        L = oracle.LIMBS[fid]
+        kw = {}
+        for n in MULTIEXP_LENGTHS:
+            a = _seeded_elements(fid, n, 0x5EED0300 + 16 * fid + n % 16).reshape(n, L) if n else \
+                np.zeros((0, L), dtype=np.uint32)
+            b = _seeded_elements(fid, n, 0x5EED0380 + 16 * fid + n % 16).reshape(n, L) if n else \
+                np.zeros((0, L), dtype=np.uint32)
+            a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+            kw[f"a_{n}"], kw[f"b_{n}"] = a, b
+            for mode in (0, 1):
+                out = np.zeros(L, dtype=np.uint32)
+                rc = ref.ref_multi_exp_oracle_field(fid, p_(a), p_(b), n, mode, p_(out))
+                assert rc == 0
+                kw[f"out_{n}_mode{mode}"] = out
+        np.savez_compressed(HERE / f"ref_multiexp_{FIELD_NAMES[fid]}.npz", lengths=np.array(MULTIEXP_LENGTHS), **kw)
+
+
 def main() -> None:
     ref = oracle.ref()
     if ref is None:
         raise SystemExit("reference checkout not found; cannot generate golden fixtures")
+    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "multiexp":
+        write_multiexp(ref)
+        print("multiexp fixtures written to", HERE)
+        return
     p_ = oracle._ptr
 
     # 1. Scalar operator KATs
@@ -108,6 +139,8 @@ def main() -> None:
             outs["serial" if serial else "parallel"] = y
         np.savez_compressed(HERE / f"ref_butterfly_{FIELD_NAMES[fid]}.npz", x=x, omega=wl, log_cpus=2,
                             **outs)
+    # 5. multi-exponentiation
+    write_multiexp(ref)
     print("golden fixtures written to", HERE)
 
 

@@ -108,6 +108,13 @@ def test_entry_points_validate_before_touching_the_gpu(gsn):
         (lambda: lib.gsn_autotune(9, 8, 10, 3), FIELD, b"unknown field"),
         (lambda: lib.gsn_tuning_load(b"/nonexistent/tuning.json"), ARG, b"cannot read"),
         (lambda: lib.gsn_plan_describe(1, 10, ctypes.create_string_buffer(4), 4), ARG, b"too small"),
+        (lambda: lib.gsn_multiexp(9, fake, fake, 16, fake, 0, None), FIELD, b"unknown field"),
+        (lambda: lib.gsn_multiexp(1, fake, fake, 16, fake, 5, None), ARG, b"mode"),
+        (lambda: lib.gsn_multiexp(1, fake, fake, 16, None, 0, None), ARG, b"null output"),
+        (lambda: lib.gsn_multiexp(1, None, fake, 16, fake, 0, None), ARG, b"null input"),
+        (lambda: lib.gsn_multiexp(1, ctypes.c_void_p(0x10004), fake, 16, fake, 0, None), ARG, b"aligned"),
+        (lambda: lib.gsn_multiexp(1, fake, fake, (1 << 40) + 1, fake, 0, None), SIZE, b"exceeds"),
+        (lambda: lib.gsn_multiexp_host(1, None, None, 16, fake, 0), ARG, b"null input"),
     ]
     for i, (call, want, msg) in enumerate(cases):
         rc = call()

@@ -39,3 +39,32 @@ def test_cpp_best_fft(gsn, cuda_device, dropin_exe, tmp_path, fid, log_n):
     assert r.returncode == 0, r.stderr
     got = np.fromfile(fout, dtype=np.uint32).reshape(x.shape)
     assert np.array_equal(got, O.ntt(fid, x).reshape(x.shape))
+
+
+@pytest.fixture(scope="module")
+def multiexp_exe(tmp_path_factory, gsn):
+    if not shutil.which("g++"):
+        pytest.skip("g++ not available")
+    libdir = gsn.library_path().parent
+    exe = tmp_path_factory.mktemp("cpp") / "multiexp_dropin"
+    subprocess.run(["g++", "-std=c++17", "-O2", f"-I{ROOT / 'include'}", str(ROOT / "tests/cpp/multiexp_dropin.cpp"),
+                    f"-L{libdir}", "-lgpusnarks_gb300", f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    return exe
+
+
+@pytest.mark.parametrize("fid,n", [(0, 1000), (1, 777), (2, 129)])
+def test_cpp_multiexp(gsn, cuda_device, multiexp_exe, tmp_path, fid, n):
+    """multiexp<FieldT, FieldMul>(a, mul) called as the reference's test/main.cpp:118 does: the Montgomery
+    product of the stored words summed, and the canonical form, both equal to the oracle."""
+    f = gsn.BY_ID[fid]
+    a = f.random_array(n, seed=0x5EED0710 + fid)
+    b = f.random_array(n, seed=0x5EED0720 + fid)
+    fa, fb, fo = tmp_path / "a.bin", tmp_path / "b.bin", tmp_path / "out.bin"
+    a.tofile(fa)
+    b.tofile(fb)
+    r = subprocess.run([str(multiexp_exe), str(fid), str(n), str(fa), str(fb), str(fo)],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stderr
+    got = np.fromfile(fo, dtype=np.uint32).reshape(2, f.limbs)
+    assert np.array_equal(got[0], O.multiexp(fid, a, b, O.MULTIEXP_MONTGOMERY))
+    assert np.array_equal(got[1], O.multiexp(fid, a, b, O.MULTIEXP_CANONICAL))

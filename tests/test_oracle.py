@@ -194,3 +194,34 @@ def test_against_compiled_reference_when_present():
         y = x.copy()
         ref.ref_fft_oracle_field(fid, O._ptr(y), log_n, O._ptr(wl), 3, 0, 0)
         assert (O.fft(fid, x, w, log_cpus=3, ref_butterfly=True) == y).all()
+
+
+@pytest.mark.parametrize("fid,name", [(0, "p32"), (1, "bls12_381_fr"), (2, "mnt4753_fr")])
+def test_multiexp_oracle_against_reference_fixtures(fid, name):
+    """The restated multi_exp (test/multiexp.h:3-13) equals the compiled reference's own multi_exp over
+    the same field type (golden fixtures) and the definition sum a_i b_i (Python integers)."""
+    g = np.load(pathlib.Path(__file__).parent / "golden" / f"ref_multiexp_{name}.npz")
+    for n in g["lengths"]:
+        a, b = g[f"a_{n}"], g[f"b_{n}"]
+        for mode in (0, 1):
+            got = O.multiexp(fid, a, b, mode)
+            assert np.array_equal(got, g[f"out_{n}_mode{mode}"]), (n, mode)
+            if n <= 257:
+                assert O.from_limbs(got) == O.multiexp_definition(fid, a, b, mode), (n, mode)
+
+
+def test_multiexp_oracle_against_compiled_reference_when_present():
+    ref = O.ref()
+    if ref is None:
+        pytest.skip("reference checkout not present")
+    import random
+    for fid in (0, 1, 2):
+        rnd = random.Random(77 + fid)
+        p = O.MODULI[fid]
+        n = 333
+        a = O.array(fid, [rnd.randrange(p) for _ in range(n)])
+        b = O.array(fid, [rnd.randrange(p) for _ in range(n)])
+        for mode in (0, 1):
+            out = np.zeros(O.LIMBS[fid], dtype=np.uint32)
+            assert ref.ref_multi_exp_oracle_field(fid, O._ptr(a), O._ptr(b), n, mode, O._ptr(out)) == 0
+            assert np.array_equal(O.multiexp(fid, a, b, mode), out)
