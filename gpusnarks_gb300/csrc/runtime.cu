@@ -311,6 +311,22 @@ static void default_root(const FieldOps& F, int log_n, uint32_t* out) {
   std::memcpy(out, it->second.data(), it->second.size());
 }
 
+// Field inverse (canonical in and out), memoised: one costs a full host exponentiation (about a
+// millisecond for the 753-bit field), and every inverse or coset-inverse transform needs n^-1 or s^-1.
+static void inv_memo(const FieldOps& F, const uint32_t* x, uint32_t* out) {
+  static std::mutex mu;
+  static std::map<std::pair<int, std::string>, std::string> memo;
+  const std::string key = limbs_key(x, F.limbs);
+  std::lock_guard<std::mutex> g(mu);
+  auto it = memo.find(std::make_pair(F.id, key));
+  if (it == memo.end()) {
+    uint32_t r[kMaxLimbs] = {0};
+    F.inv(x, r);
+    it = memo.emplace(std::make_pair(F.id, key), limbs_key(r, F.limbs)).first;
+  }
+  std::memcpy(out, it->second.data(), it->second.size());
+}
+
 // Returns a cached table of base^e * R for e in [0, 2^log_count); builds it
 // on first use.  Caller holds no lock.
 static int powers_table(const FieldOps& F, const uint32_t* base, int log_count, const uint32_t** out) {
@@ -386,7 +402,7 @@ int resolve_tables(const FieldOps& F, uint32_t log_n, const uint32_t* omega, int
       nn[0] = 0;
       nn[log_n / 32] = 1u << (log_n % 32);
     }
-    F.inv(nn, ninv);
+    inv_memo(F, nn, ninv);
     F.to_mont(ninv, T->pre_const);
     T->has_pre_const = 1;
   }
@@ -405,7 +421,7 @@ int resolve_tables(const FieldOps& F, uint32_t log_n, const uint32_t* omega, int
       rc = powers_table(F, s, (int)log_n, &T->pre_table);
     } else {
       uint32_t si[kMaxLimbs];
-      F.inv(s, si);
+      inv_memo(F, s, si);
       rc = powers_table(F, si, (int)log_n, &T->post_table);
     }
     if (rc) return rc;
@@ -433,7 +449,7 @@ bool find_default_twiddles(const FieldOps& F, int log_n, const uint32_t** tw, in
 int resolve_p32_tables(const FieldOps& F, const Plan& plan, Tables* T) {
   uint32_t root[kMaxLimbs];
   std::memcpy(root, T->root, sizeof(uint32_t) * F.limbs);
-  if (T->inverse) F.inv(T->root, root);
+  if (T->inverse) inv_memo(F, T->root, root);
   const int L = plan.log_n;
   for (int p = 0; p < plan.npass; ++p) {
     const int r = plan.radix_log[p];
@@ -598,7 +614,7 @@ static int coset_z_inv(const FieldOps& F, uint32_t log_n, const uint32_t* shift,
   for (int i = 0; i < F.limbs; ++i) {  // t - 1; t >= 2 here
     if (t[i]--) break;
   }
-  F.inv(t, u);
+  inv_memo(F, t, u);
   F.to_mont(u, t);
   F.to_mont(t, zr2);
   return GSN_OK;
@@ -833,12 +849,22 @@ int gsn_ntt_host_batch(int field, uint32_t* const* data, size_t count, uint32_t 
 // ---------------------------------------------------------------------------
 namespace gsn {
 // The representation constant of multiexp.cuh: 2^(32(2N+1)) mod p (canonical) or 2^(32(N+1)) mod p
-// (Montgomery), canonical limbs.
+// (Montgomery), canonical limbs.  Computed once per (field, mode): the host exponentiation takes longer
+// than a whole small multi-exponentiation on the GPU.
 static void multiexp_fix(const FieldOps& F, int mode, uint32_t* fix) {
-  uint32_t two[kMaxLimbs] = {0};
-  two[0] = 2;
-  const int N = F.limbs;
-  F.pow(two, (uint64_t)32 * (mode == GSN_MULTIEXP_CANONICAL ? 2 * N + 1 : N + 1), fix);
+  static std::mutex mu;
+  static std::map<std::pair<int, int>, std::string> memo;
+  std::lock_guard<std::mutex> g(mu);
+  auto key = std::make_pair(F.id, mode);
+  auto it = memo.find(key);
+  if (it == memo.end()) {
+    uint32_t two[kMaxLimbs] = {0}, r[kMaxLimbs] = {0};
+    two[0] = 2;
+    const int N = F.limbs;
+    F.pow(two, (uint64_t)32 * (mode == GSN_MULTIEXP_CANONICAL ? 2 * N + 1 : N + 1), r);
+    it = memo.emplace(key, limbs_key(r, N)).first;
+  }
+  std::memcpy(fix, it->second.data(), it->second.size());
 }
 
 static int multiexp_impl(const FieldOps& F, const uint32_t* a, const uint32_t* b, uint64_t n, uint32_t* out,

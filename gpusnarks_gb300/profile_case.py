@@ -3,6 +3,7 @@
     python -m gpusnarks_gb300.profile_case --field p32 --log-n 24 --reps 3
     python -m gpusnarks_gb300.profile_case --field bls12_381_fr --batch 512 --batch-lo 10 --batch-hi 18
     python -m gpusnarks_gb300.profile_case --microbench imad --iters 2000
+    python -m gpusnarks_gb300.profile_case --multiexp 24 --field bls12_381_fr --reps 1 --warmup 1
 
 Fills the input on the device (gsn_fill_random), runs `warmup` untimed and
 `reps` further transforms through the C ABI, prints the mean event time.
@@ -28,6 +29,7 @@ def main() -> None:
     ap.add_argument("--microbench", default="", choices=["", "imad", "imad_wide", "imad_lo", "imad_hi"],
                     help="run one integer multiply-add microbenchmark instead (--iters steps per thread)")
     ap.add_argument("--iters", type=int, default=2000)
+    ap.add_argument("--multiexp", type=int, default=0, help="log2 n: run gsn_multiexp on 2^n elements instead")
     args = ap.parse_args()
 
     import torch
@@ -37,6 +39,9 @@ def main() -> None:
 
     if args.microbench:
         run_microbench(g, args)
+        return
+    if args.multiexp:
+        run_multiexp(g, torch, args)
         return
     f = g.FIELDS[args.field]
     if args.batch:
@@ -57,6 +62,29 @@ def main() -> None:
     ms = s.elapsed_time(e) / max(args.reps, 1)
     print(f"{args.field} 2^{args.log_n}: {ms:.4f} ms per transform, {n / ms / 1e3:.1f} Melem/s")
 
+
+
+def run_multiexp(g, torch, args) -> None:
+    """gsn_multiexp over 2^multiexp seeded elements (two launches per call)."""
+    from gpusnarks_gb300.batch import fill_random
+    f = g.FIELDS[args.field]
+    n = 1 << args.multiexp
+    a = torch.empty(n * f.limbs, dtype=torch.int32, device="cuda")
+    b = torch.empty(n * f.limbs, dtype=torch.int32, device="cuda")
+    fill_random(f, a, 0x5EED0600)
+    fill_random(f, b, 0x5EED0700)
+    out = torch.empty(f.limbs, dtype=torch.int32, device="cuda")
+    for _ in range(args.warmup):
+        g.multiexp(f, a, b, out)
+    torch.cuda.synchronize()
+    s, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    s.record()
+    for _ in range(args.reps):
+        g.multiexp(f, a, b, out)
+    e.record()
+    torch.cuda.synchronize()
+    ms = s.elapsed_time(e) / max(args.reps, 1)
+    print(f"{args.field} multiexp 2^{args.multiexp}: {ms:.4f} ms, {n / ms / 1e6:.2f} G elements/s")
 
 
 def run_microbench(g, args) -> None:
