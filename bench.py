@@ -238,13 +238,13 @@ def imad_peak(g) -> dict:
 
 def montgomery_schedules(g, iters: int = 2000) -> dict:
     """Montgomery products per second on the whole GPU for the one-thread schedules (0 row chains,
-    1 even/odd accumulators merged every row, 2 split accumulators with a carried merge) and the
-    24-limb product split over 2 or 4 cooperating lanes."""
+    1 even/odd accumulators merged every row, the kernels' default) and the 24-limb product split over
+    2 or 4 cooperating lanes."""
     lib = g.load()
     out = {}
     for name, fid in (("bls12_381_fr", 1), ("mnt4753_fr", 2)):
         per = {}
-        for sched in (0, 1, 2):
+        for sched in (0, 1):
             v = ctypes.c_double()
             g._lib.check(lib.gsn_microbench_mont(fid, sched, iters, ctypes.byref(v)))
             per[f"thread_schedule{sched}_G_per_s"] = round(v.value / 1e9, 3)
@@ -716,6 +716,8 @@ def run_gpu(args, rank, local, ws):
         extra["poly_product_2^21"] = poly_product_2_21(g, torch)
         extra["multiexp"] = multiexp_bench(g, torch, hbm_gbs, ip["mads_per_s"])
         extra["hbm_peak_gbs"] = hbm_gbs
+        extra["hbm_peak_source"] = ("measured: MEASURED_PEAKS.json hbm_gbs (STREAM-style copy on this pool's GB300)"
+                                    if "hbm_gbs" in pk else "fallback: 6.8 TB/s, one earlier GB300 measurement")
         try:
             extra["bls12_381_batch_4096"] = batch_vs_per_call(g, torch)
         except Exception as exc:  # report, do not hide

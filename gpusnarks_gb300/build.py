@@ -8,8 +8,7 @@ or when the build-time options below change.
 
 Build-time options (environment variables, passed to nvcc as -D defines):
   GSN_MONT_SCHEDULE  Montgomery product schedule of the multi-limb fields:
-                     1 even/odd accumulators (default), 0 row chains,
-                     2 split accumulators with a carried merge.
+                     1 even/odd accumulators (default), 0 row chains.
 """
 from __future__ import annotations
 

@@ -312,114 +312,8 @@ __device__ __forceinline__ void fe_mul_eo(Fe<P>& r, const Fe<P>& a, const Fe<P>&
   for (int j = 0; j < N; ++j) r.l[j] = (t[j] & mask) | (d[j] & ~mask);
 }
 
-// ---------------------------------------------------------------------------
-// Split-accumulator CIOS with a carried merge.  Same result, fewer
-// instructions than fe_mul_eo: both accumulators stay aligned at word 0,
-// T = A + B, A taking the even-limb products (word pairs (0,1), (2,3), ...)
-// and B the odd-limb ones (pairs (1,2), (3,4), ...).  After a row's
-// reduction A_0 + B_0 = 0 mod 2^32, so T / 2^32 = (A >> 32) + (B >> 32) + c
-// with c the carry of A_0 + B_0: one add.cc produces c in the carry flag and
-// the next row's first multiply-add chain (madc) consumes it; the shifts are
-// register renaming.  Per row 4N + 7 instructions instead of 4N + 30.
-// Bounds: T < 2^33 p < 2^(32 (N + 1)) for the fields here, so A fits N + 1
-// words and B N + 2 (its top pair ends one word higher).
-// ---------------------------------------------------------------------------
-
-// acc[0..N] += sum_k x[2k] * y * 2^(64 k), the chain's first step taking the carry flag in when cin
-template <int N, bool CIN>
-__device__ __forceinline__ void even_chain(uint32_t (&acc)[N + 2], const uint32_t* x, uint32_t y) {
-  if constexpr (CIN) ptx::madc_lo_cc(acc[0], x[0], y, acc[0]);
-  else ptx::mad_lo_cc(acc[0], x[0], y, acc[0]);
-  ptx::madc_hi_cc(acc[1], x[0], y, acc[1]);
-#pragma unroll
-  for (int k = 1; k < N / 2; ++k) {
-    ptx::madc_lo_cc(acc[2 * k], x[2 * k], y, acc[2 * k]);
-    ptx::madc_hi_cc(acc[2 * k + 1], x[2 * k], y, acc[2 * k + 1]);
-  }
-  ptx::addc(acc[N], acc[N], 0u);
-}
-// acc[1..N+1] += sum_k x[2k+1] * y * 2^(64 k + 32)
-template <int N>
-__device__ __forceinline__ void odd_chain(uint32_t (&acc)[N + 2], const uint32_t* x, uint32_t y) {
-  ptx::mad_lo_cc(acc[1], x[1], y, acc[1]);
-  ptx::madc_hi_cc(acc[2], x[1], y, acc[2]);
-#pragma unroll
-  for (int k = 1; k < N / 2; ++k) {
-    ptx::madc_lo_cc(acc[2 * k + 1], x[2 * k + 1], y, acc[2 * k + 1]);
-    ptx::madc_hi_cc(acc[2 * k + 2], x[2 * k + 1], y, acc[2 * k + 2]);
-  }
-  ptx::addc(acc[N + 1], acc[N + 1], 0u);
-}
-template <class P>
-__device__ __forceinline__ void even_chain_mod(uint32_t (&acc)[P::N + 2], uint32_t y) {
-  constexpr int N = P::N;
-  ptx::mad_lo_cc(acc[0], P::mod(0), y, acc[0]);
-  ptx::madc_hi_cc(acc[1], P::mod(0), y, acc[1]);
-#pragma unroll
-  for (int k = 1; k < N / 2; ++k) {
-    ptx::madc_lo_cc(acc[2 * k], P::mod(2 * k), y, acc[2 * k]);
-    ptx::madc_hi_cc(acc[2 * k + 1], P::mod(2 * k), y, acc[2 * k + 1]);
-  }
-  ptx::addc(acc[N], acc[N], 0u);
-}
-template <class P>
-__device__ __forceinline__ void odd_chain_mod(uint32_t (&acc)[P::N + 2], uint32_t y) {
-  constexpr int N = P::N;
-  ptx::mad_lo_cc(acc[1], P::mod(1), y, acc[1]);
-  ptx::madc_hi_cc(acc[2], P::mod(1), y, acc[2]);
-#pragma unroll
-  for (int k = 1; k < N / 2; ++k) {
-    ptx::madc_lo_cc(acc[2 * k + 1], P::mod(2 * k + 1), y, acc[2 * k + 1]);
-    ptx::madc_hi_cc(acc[2 * k + 2], P::mod(2 * k + 1), y, acc[2 * k + 2]);
-  }
-  ptx::addc(acc[N + 1], acc[N + 1], 0u);
-}
-
-template <class P>
-__device__ __forceinline__ void fe_mul_ab(Fe<P>& r, const Fe<P>& a, const Fe<P>& b) {
-  constexpr int N = P::N;
-  static_assert(N % 2 == 0, "split-accumulator schedule needs an even limb count");
-  uint32_t A[N + 2], B[N + 2];
-#pragma unroll
-  for (int j = 0; j < N + 2; ++j) A[j] = B[j] = 0u;
-#pragma unroll
-  for (int i = 0; i < N; ++i) {
-    // the carry flag holds c of the previous row here (rows i > 0)
-    if (i == 0) even_chain<N, false>(A, a.l, b.l[i]);
-    else even_chain<N, true>(A, a.l, b.l[i]);
-    odd_chain<N>(B, a.l, b.l[i]);
-    const uint32_t m = (A[0] + B[0]) * P::PINV;
-    even_chain_mod<P>(A, m);
-    odd_chain_mod<P>(B, m);
-    uint32_t junk;
-    ptx::add_cc(junk, A[0], B[0]);  // = 0 mod 2^32; the carry flag keeps c for the next chain
-    (void)junk;
-#pragma unroll
-    for (int j = 0; j < N + 1; ++j) {
-      A[j] = A[j + 1];
-      B[j] = B[j + 1];
-    }
-    A[N + 1] = 0u;
-    B[N + 1] = 0u;
-  }
-  // t = A + B + c  (< 2p), then one conditional subtraction
-  uint32_t t[N + 1];
-  ptx::addc_cc(t[0], A[0], B[0]);
-#pragma unroll
-  for (int j = 1; j < N; ++j) ptx::addc_cc(t[j], A[j], B[j]);
-  ptx::addc(t[N], A[N], B[N]);
-  uint32_t d[N], mask;
-  ptx::sub_cc(d[0], t[0], P::mod(0));
-#pragma unroll
-  for (int j = 1; j < N; ++j) ptx::subc_cc(d[j], t[j], P::mod(j));
-  ptx::subc(mask, t[N], 0u);
-#pragma unroll
-  for (int j = 0; j < N; ++j) r.l[j] = (t[j] & mask) | (d[j] & ~mask);
-}
-
-// Montgomery product used by the kernels.  kMontSchedule selects the
-// multi-limb schedule: 1 = even/odd accumulators (default), 0 = row chains,
-// 2 = split accumulators with a carried merge.
+// Montgomery product used by the kernels.  GSN_MONT_SCHEDULE selects the
+// multi-limb schedule: 1 = even/odd accumulators (default), 0 = row chains.
 #ifndef GSN_MONT_SCHEDULE
 #define GSN_MONT_SCHEDULE 1
 #endif
@@ -429,8 +323,6 @@ __device__ __forceinline__ void fe_mul(Fe<P>& r, const Fe<P>& a, const Fe<P>& b)
     r.l[0] = mul1<P>(a.l[0], b.l[0]);
   } else if constexpr (S == 1 && P::N % 2 == 0) {
     fe_mul_eo<P>(r, a, b);
-  } else if constexpr (S == 2 && P::N % 2 == 0) {
-    fe_mul_ab<P>(r, a, b);
   } else {
     fe_mul_rows<P>(r, a, b);
   }

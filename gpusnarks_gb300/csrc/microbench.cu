@@ -602,15 +602,13 @@ extern "C" int gsn_microbench_mont_coop(int field, int lanes, int iters, double*
 }
 
 extern "C" int gsn_microbench_mont(int field, int schedule, int iters, double* muls_per_s) {
-  if (iters <= 0 || !muls_per_s || schedule < 0 || schedule > 2)
+  if (iters <= 0 || !muls_per_s || schedule < 0 || schedule > 1)
     return set_error(GSN_ERR_ARG, "bad microbenchmark arguments");
-  switch (field * 3 + schedule) {
-    case GSN_BLS12_381_FR * 3 + 0: return run_mont_bench<FieldBLS12_381, 0>(iters, muls_per_s);
-    case GSN_BLS12_381_FR * 3 + 1: return run_mont_bench<FieldBLS12_381, 1>(iters, muls_per_s);
-    case GSN_BLS12_381_FR * 3 + 2: return run_mont_bench<FieldBLS12_381, 2>(iters, muls_per_s);
-    case GSN_MNT4753_FR * 3 + 0: return run_mont_bench<FieldMNT4_753, 0>(iters, muls_per_s);
-    case GSN_MNT4753_FR * 3 + 1: return run_mont_bench<FieldMNT4_753, 1>(iters, muls_per_s);
-    case GSN_MNT4753_FR * 3 + 2: return run_mont_bench<FieldMNT4_753, 2>(iters, muls_per_s);
+  switch (field * 2 + schedule) {
+    case GSN_BLS12_381_FR * 2 + 0: return run_mont_bench<FieldBLS12_381, 0>(iters, muls_per_s);
+    case GSN_BLS12_381_FR * 2 + 1: return run_mont_bench<FieldBLS12_381, 1>(iters, muls_per_s);
+    case GSN_MNT4753_FR * 2 + 0: return run_mont_bench<FieldMNT4_753, 0>(iters, muls_per_s);
+    case GSN_MNT4753_FR * 2 + 1: return run_mont_bench<FieldMNT4_753, 1>(iters, muls_per_s);
     default: return set_error(GSN_ERR_FIELD, "Montgomery microbenchmark covers the multi-limb fields");
   }
 }

@@ -370,8 +370,8 @@ int gsn_microbench_imad(int iters, double* mads_per_s, double* mads_per_clk_sm, 
  * gsn_microbench_imad with what the multiply pipe issues without carries. */
 int gsn_microbench_imad_form(int form, int iters, double* ops_per_s);
 /* Throughput (products per second, all SMs) of the multi-limb Montgomery
- * product with schedule 0 (row chains), 1 (even/odd accumulators merged every
- * row) or 2 (split accumulators, carried merge); first checks 256 products of
+ * product with schedule 0 (row chains) or 1 (even/odd accumulators, the
+ * kernels' default); first checks 256 products of
  * that schedule against the host arithmetic (GSN_ERR_STATE on a mismatch). */
 int gsn_microbench_mont(int field, int schedule, int iters, double* muls_per_s);
 /* Same for the cooperative MNT4-753 product split over `lanes` (2 or 4)
