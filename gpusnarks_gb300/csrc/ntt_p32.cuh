@@ -369,6 +369,14 @@ __device__ __forceinline__ void prefetch_columns(const P32Args& A, uint4* buf, u
   }
 }
 
+// Register cap of the fixed-radix kernels: 64 for 8-row sub-steps, so 8 CTAs of 128 threads fit an SM by
+// registers (86 uncapped for radix 2^9, 5 CTAs); measured on GB300 at 2^24 / 2^26 / 2^28: 0.186 / 0.698 /
+// 2.985 ms capped against 0.192 / 0.713 / 3.093 ms uncapped, despite ~50 bytes of spills at radix 2^9.
+template <int ET>
+constexpr int max_regs() {
+  return ET == 3 ? 64 : 128;
+}
+
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
@@ -404,7 +412,7 @@ __device__ __forceinline__ void store_fourstep(const P32Args& A, const uint4* sm
 // streams into the other buffer with cp.async.  The trailing __syncthreads of an iteration ends all reads
 // of the buffer the next iteration starts filling.  Same arithmetic and results as ntt_p32_fixed_kernel.
 template <int RL, int ET, int LCG>
-__global__ void __launch_bounds__(512) ntt_p32_pipe_kernel(const __grid_constant__ P32Args A) {
+__global__ void __launch_bounds__(512) __maxnreg__(p32::max_regs<ET>()) ntt_p32_pipe_kernel(const __grid_constant__ P32Args A) {
   using namespace p32;
   extern __shared__ uint4 gsn_smem[];
   constexpr uint32_t CG = 1u << LCG;
@@ -450,7 +458,7 @@ __global__ void __launch_bounds__(512) ntt_p32_pipe_kernel(const __grid_constant
 }
 
 template <int RL, int ET, int LCG>
-__global__ void __launch_bounds__(512) ntt_p32_fixed_kernel(const __grid_constant__ P32Args A) {
+__global__ void __launch_bounds__(512) __maxnreg__(p32::max_regs<ET>()) ntt_p32_fixed_kernel(const __grid_constant__ P32Args A) {
   using namespace p32;
   extern __shared__ uint4 gsn_smem[];
   uint4* sm = gsn_smem;
