@@ -184,8 +184,16 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
   }
 }
 
+// Register cap of the per-pass kernel (255: none).  The 24-limb tile needs 112 registers uncapped, so 4 CTAs
+// of 128 threads per SM; at 102 a fifth fits (about 50 bytes of spills).  Measured on GB300, MNT4-753
+// 2^20 / 2^21 / 2^22: 1.435 / 2.821 / 5.985 ms capped against 1.470 / 2.881 / 6.277 ms uncapped; 2^18 the same.
 template <class P>
-__global__ void ntt_pass_kernel(const __grid_constant__ PassArgs A) {
+constexpr int pass_max_regs() {
+  return P::N >= 16 ? 102 : 255;
+}
+
+template <class P>
+__global__ void __maxnreg__(pass_max_regs<P>()) ntt_pass_kernel(const __grid_constant__ PassArgs A) {
   extern __shared__ uint4 gsn_smem[];
   uint32_t* sm = reinterpret_cast<uint32_t*>(gsn_smem);
   for (uint64_t t = blockIdx.x; t < A.tiles; t += gridDim.x) ntt_tile<P>(A, t, sm);
