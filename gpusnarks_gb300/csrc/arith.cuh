@@ -274,8 +274,10 @@ __device__ __forceinline__ void pair_chain_mod(uint32_t (&acc)[P::N + 1], int of
 // 3 carry-chain adds per row instead of N+1 for a full merge, no branch: the carry-chain adds occupy the
 // same multiply pipe as the products on this GPU, and the full merge cost the 24-limb product a quarter of
 // its pipe time (6.1 against 8.3 G products/s in isolation).
-template <class P>
-__device__ __forceinline__ void fe_mul_eo(Fe<P>& r, const Fe<P>& a, const Fe<P>& b) {
+// `row(i)` returns limb i of b, the multiplier of row i; the two forms below read it from registers or from
+// memory.
+template <class P, class Row>
+__device__ __forceinline__ void fe_mul_eo_rows(Fe<P>& r, const Fe<P>& a, Row row) {
   constexpr int N = P::N;
   static_assert(N % 2 == 0 && N >= 4, "even/odd schedule needs an even limb count of at least 4");
   uint32_t E[N + 1], O[N + 1];
@@ -284,8 +286,9 @@ __device__ __forceinline__ void fe_mul_eo(Fe<P>& r, const Fe<P>& a, const Fe<P>&
   for (int j = 0; j <= N; ++j) E[j] = O[j] = 0u;
 #pragma unroll
   for (int i = 0; i < N; ++i) {
-    pair_chain<N>(E, a.l, 0, b.l[i]);
-    pair_chain<N>(O, a.l, 1, b.l[i]);
+    const uint32_t bi = row(i);
+    pair_chain<N>(E, a.l, 0, bi);
+    pair_chain<N>(O, a.l, 1, bi);
     const uint32_t m = E[0] * P::PINV;
     pair_chain_mod<P>(E, 0, m);
     pair_chain_mod<P>(O, 1, m);
@@ -324,6 +327,19 @@ __device__ __forceinline__ void fe_mul_eo(Fe<P>& r, const Fe<P>& a, const Fe<P>&
   for (int j = 0; j < N; ++j) r.l[j] = (t[j] & mask) | (d[j] & ~mask);
 }
 
+template <class P>
+__device__ __forceinline__ void fe_mul_eo(Fe<P>& r, const Fe<P>& a, const Fe<P>& b) {
+  fe_mul_eo_rows<P>(r, a, [&](int i) { return b.l[i]; });
+}
+
+// The same product with b's limbs loaded from memory one row at a time, so b takes no registers across the
+// product: one register per row instead of N for the whole product.  The 24-limb per-pass tile uses it to fit
+// five CTAs of 128 threads per SM (96 registers, no spills) where the register operand needs 112.
+template <class P>
+__device__ __forceinline__ void fe_mul_eo_mem(Fe<P>& r, const Fe<P>& a, const uint32_t* b) {
+  fe_mul_eo_rows<P>(r, a, [=](int i) { return b[i]; });
+}
+
 // Montgomery product used by the kernels.  GSN_MONT_SCHEDULE selects the
 // multi-limb schedule: 1 = even/odd accumulators (default), 0 = row chains.
 #ifndef GSN_MONT_SCHEDULE
@@ -337,6 +353,20 @@ __device__ __forceinline__ void fe_mul(Fe<P>& r, const Fe<P>& a, const Fe<P>& b)
     fe_mul_eo<P>(r, a, b);
   } else {
     fe_mul_rows<P>(r, a, b);
+  }
+}
+
+// r = a * b R^-1 with b's limbs in memory (any address space).  The even/odd schedule reads them row by row;
+// the others load b first.
+template <class P, int S = GSN_MONT_SCHEDULE>
+__device__ __forceinline__ void fe_mul_mem(Fe<P>& r, const Fe<P>& a, const uint32_t* b) {
+  if constexpr (S == 1 && P::N % 2 == 0 && P::N >= 4) {
+    fe_mul_eo_mem<P>(r, a, b);
+  } else {
+    Fe<P> w;
+#pragma unroll
+    for (int l = 0; l < P::N; ++l) w.l[l] = b[l];
+    fe_mul<P, S>(r, a, w);
   }
 }
 

@@ -59,8 +59,11 @@ __device__ __forceinline__ uint64_t rest_offset(uint64_t rest, int npass, const 
   return off;
 }
 
-// One tile of one pass.  `sm` holds 2^(log_r + log_j) elements.
-template <class P>
+// One tile of one pass.  `sm` holds 2^(log_r + log_j) elements.  TW_MEM: the product reads the multiplier
+// (twiddle, pre- or post-table entry) from memory row by row (fe_mul_mem) instead of loading it into registers
+// first; A must then live in addressable memory (a __grid_constant__ parameter or shared memory), since the
+// pre-scale constant is read through a pointer to A.pre_const.
+template <class P, bool TW_MEM>
 __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
   constexpr int N = P::N;
   const int lr = A.log_r, lj = A.log_j;
@@ -111,7 +114,7 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
   }
   __syncthreads();
 
-  // --- phases; every multiplication goes through the single fe_mul below, so
+  // --- phases; every multiplication goes through the single product below, so
   // the fully unrolled product exists once in the instruction stream --------
   //   ph = -1        pre-scale (first pass: coset powers or n^-1)
   //   ph = 0..lr-1   radix-2 DIF stage ph (natural in, bit-reversed out)
@@ -122,19 +125,30 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
     const int count = stage ? (R >> 1) * J : R * J;
     for (int b = tid; b < count; b += nthr) {
       Fe<P> x, w;
+      const uint32_t* wsrc = nullptr;  // TW_MEM: limbs of the multiplier
       bool mul = false;
       uint32_t* out;
+      auto take = [&](const uint32_t* src) {  // the multiplier's limbs are at src
+        if constexpr (TW_MEM) {
+          wsrc = src;
+        } else {
+          fe_load<P>(w, src);
+        }
+        mul = true;
+      };
       if (ph < 0) {
         const int k = b >> lj, jj = b & (J - 1);
         out = sm + ((k << lj) + jj) * N;
         fe_load<P>(x, out);
         if (A.pre_table) {
-          fe_load<P>(w, A.pre_table + src_pos(k, jj) * N);
+          take(A.pre_table + src_pos(k, jj) * N);
+        } else if constexpr (TW_MEM) {
+          take(A.pre_const);
         } else {
 #pragma unroll
-          for (int l = 0; l < N; ++l) w.l[l] = A.pre_const[l];
+          for (int l = 0; l < N; ++l) w.l[l] = A.pre_const[l];  // 4-byte aligned in PassArgs: no vector loads
+          mul = true;
         }
-        mul = true;
       } else if (stage) {
         // Butterfly b = (i, group, jj) with the twiddle index i slowest: the 2^(lr-1-log_half) * J
         // butterflies of twiddle 1 (i = 0) are then consecutive threads, so in the late stages whole warps
@@ -155,8 +169,7 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
         out = sm + ((v << lj) + jj) * N;
         if (i != 0) {
           const uint64_t e = ((uint64_t)i << ph) << (A.log_n - lr);
-          tw_load<P>(w, A.tw, tw_index(A.tw_log, A.log_n, A.inverse, e));
-          mul = true;
+          take(A.tw + tw_index(A.tw_log, A.log_n, A.inverse, e) * N);
         }
       } else {
         const int k = b >> lj, jj = b & (J - 1);
@@ -164,39 +177,48 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
         if (!A.last) {
           const uint64_t ex = ((jbase + jj) * (uint64_t)k) << A.log_outer;
           out = A.dst + (base + ((uint64_t)k << A.log_inner) + jj) * N;
-          if (ex != 0) {
-            tw_load<P>(w, A.tw, tw_index(A.tw_log, A.log_n, A.inverse, ex));
-            mul = true;
-          }
+          if (ex != 0) take(A.tw + tw_index(A.tw_log, A.log_n, A.inverse, ex) * N);
         } else {
           const uint64_t opos = obase + jj + ((uint64_t)k << A.log_outer);
           out = A.dst + opos * N;
-          if (A.post_table) {
-            fe_load<P>(w, A.post_table + opos * N);
-            mul = true;
-          }
+          if (A.post_table) take(A.post_table + opos * N);
         }
       }
-      if (mul) fe_mul<P>(x, x, w);
+      if (mul) {
+        if constexpr (TW_MEM) {
+          fe_mul_mem<P>(x, x, wsrc);
+        } else {
+          fe_mul<P>(x, x, w);
+        }
+      }
       fe_store<P>(out, x);
     }
     __syncthreads();
   }
 }
 
-// Register cap of the per-pass kernel (255: none).  The 24-limb tile needs 112 registers uncapped, so 4 CTAs
-// of 128 threads per SM; at 102 a fifth fits (about 50 bytes of spills).  Measured on GB300, MNT4-753
-// 2^20 / 2^21 / 2^22: 1.435 / 2.821 / 5.985 ms capped against 1.470 / 2.881 / 6.277 ms uncapped; 2^18 the same.
+// The 24-limb per-pass tile reads the multiplier from memory and is capped at 96 registers (255: no cap).
+// Registers are allocated per warp in units of 256, so 96 per thread gives 5 CTAs of 128 threads per SM
+// (20 warps) and anything from 97 to 104 only 4.  With the multiplier in registers the tile needs 112, and at
+// 96 it spills.  Measured on GB300, MNT4-753 2^18 / 2^20 / 2^22 in ms (occupancy from
+// cudaOccupancyMaxActiveBlocksPerMultiprocessor):
+//   multiplier in registers, cap 102 (4 CTAs, 48 bytes of spills):  0.3783 / 1.4354 / 5.988
+//   multiplier in registers, cap 96  (5 CTAs, 112 bytes of spills): 0.3707 / 1.4383 / 6.043
+//   multiplier from memory,  cap 96  (5 CTAs, no spills):            0.3654 / 1.4172 / 6.040
+template <class P>
+__host__ __device__ constexpr bool pass_tw_mem() {
+  return P::N >= 16;
+}
 template <class P>
 constexpr int pass_max_regs() {
-  return P::N >= 16 ? 102 : 255;
+  return P::N >= 16 ? 96 : 255;
 }
 
 template <class P>
 __global__ void __maxnreg__(pass_max_regs<P>()) ntt_pass_kernel(const __grid_constant__ PassArgs A) {
   extern __shared__ uint4 gsn_smem[];
   uint32_t* sm = reinterpret_cast<uint32_t*>(gsn_smem);
-  for (uint64_t t = blockIdx.x; t < A.tiles; t += gridDim.x) ntt_tile<P>(A, t, sm);
+  for (uint64_t t = blockIdx.x; t < A.tiles; t += gridDim.x) ntt_tile<P, pass_tw_mem<P>()>(A, t, sm);
 }
 
 // out[e] = base^e * R (Montgomery form) for e in [0, count).  `base` is
@@ -424,7 +446,7 @@ __global__ void __maxnreg__(batch_max_regs<P>())
       }
     }
     __syncthreads();
-    ntt_tile<P>(s_args, tile, sm);  // ends with __syncthreads(); s_args is rewritten only after it
+    ntt_tile<P, false>(s_args, tile, sm);  // ends with __syncthreads(); s_args is rewritten only after it
     if (threadIdx.x == 0) {
       __threadfence();
       atomicAdd(&counters[1 + (uint64_t)job * kMaxPasses + pass], 1u);
