@@ -228,7 +228,7 @@ def imad_peak(g) -> dict:
     out = {"mads_per_s": a.value, "mads_per_clk_sm": b.value, "sm_mhz": c.value}
     # the carry-free forms beside it: instructions per second, and per SM per clock at the same clock
     sms = max(1, int(__import__("torch").cuda.get_device_properties(0).multi_processor_count))
-    for form, name in ((1, "mad_wide"), (2, "mad_lo"), (3, "mad_hi")):
+    for form, name in ((1, "mad_wide"), (2, "mad_lo"), (3, "mad_hi"), (4, "add_chain")):
         v = ctypes.c_double()
         g._lib.check(lib.gsn_microbench_imad_form(form, 20000, ctypes.byref(v)))
         out[f"{name}_per_s"] = v.value

@@ -162,12 +162,30 @@ __device__ __forceinline__ void fe_sub(Fe<P>& r, const Fe<P>& a, const Fe<P>& b)
   }
 }
 
+// -p^-1 mod 2^32, the factor of each reduction row's m = t_0 * (-p^-1).  For a modulus with p_0 = 1
+// (BLS12-381 r) it is 0xFFFFFFFF.  When the compiler can see that value it rewrites m = -t_0 and the
+// reduction row that uses m, at a cost of about 44 more multiply-pipe instructions per 8-limb product
+// (measured on GB300: 180.5 against 139.5 per product, 57 against 64 G products/s, the same outputs).
+// There the factor is read from constant memory, whose contents the compiler does not assume; every
+// other field keeps the immediate.
+template <class P>
+__constant__ uint32_t c_row_pinv = P::PINV;
+
+template <class P>
+__device__ __forceinline__ uint32_t row_pinv() {
+  if constexpr (P::N > 1 && P::PINV == 0xFFFFFFFFu) {
+    return c_row_pinv<P>;
+  } else {
+    return P::PINV;
+  }
+}
+
 // One CIOS reduction step on the accumulator t[0..N+1]: m = t0 * (-p^-1),
 // t += m*p (t0 becomes 0), then t >>= 32.
 template <class P>
 __device__ __forceinline__ void cios_reduce_step(uint32_t (&t)[P::N + 2]) {
   constexpr int N = P::N;
-  const uint32_t m = t[0] * P::PINV;
+  const uint32_t m = t[0] * row_pinv<P>();
   ptx::mad_lo_cc(t[0], m, P::mod(0), t[0]);
 #pragma unroll
   for (int j = 1; j < N; ++j) ptx::madc_lo_cc(t[j], m, P::mod(j), t[j]);
@@ -271,9 +289,9 @@ __device__ __forceinline__ void pair_chain_mod(uint32_t (&acc)[P::N + 1], int of
 // row's frame), instead of running through all N+1 words.  A row's products and reduction do not touch
 // that word's position before the next merge, where the shift has brought q down to the second word:
 // that merge adds it there (addc with q as the addend), and the final combination adds the last q once.
-// 3 carry-chain adds per row instead of N+1 for a full merge, no branch: the carry-chain adds occupy the
-// same multiply pipe as the products on this GPU, and the full merge cost the 24-limb product a quarter of
-// its pipe time (6.1 against 8.3 G products/s in isolation).
+// 3 carry-chain adds per row instead of N+1 for a full merge, no branch.  The adds run on the ALU pipe, but a
+// full merge is a serial chain of N+1 dependent adds between one row's products and the next row's, and it
+// cost the 24-limb product a quarter of its time (6.1 against 8.3 G products/s in isolation on GB300).
 // `row(i)` returns limb i of b, the multiplier of row i; the two forms below read it from registers or from
 // memory.
 template <class P, class Row>
@@ -289,7 +307,7 @@ __device__ __forceinline__ void fe_mul_eo_rows(Fe<P>& r, const Fe<P>& a, Row row
     const uint32_t bi = row(i);
     pair_chain<N>(E, a.l, 0, bi);
     pair_chain<N>(O, a.l, 1, bi);
-    const uint32_t m = E[0] * P::PINV;
+    const uint32_t m = E[0] * row_pinv<P>();
     pair_chain_mod<P>(E, 0, m);
     pair_chain_mod<P>(O, 1, m);
     // E <- O + E_1 + 2^32 q (carry out of the second word pending), O <- E_2..E_N

@@ -82,6 +82,8 @@ __global__ void imad_chain_kernel(uint32_t* sink, int iters, uint32_t x, uint32_
 //   form 1: mad.wide.u32  acc64 += a * b     (one 32x32->64 word product per instruction)
 //   form 2: mad.lo.u32    acc32 += lo(a * b)
 //   form 3: mad.hi.u32    acc32 += hi(a * b)
+//   form 4: add.cc.u32 / addc.cc.u32 / addc.u32, one 8-word carry chain acc += v per step (the carry-only adds of
+//           the Montgomery products and of the modular add and subtract; ncu shows which pipe they run on)
 // The multiplier a changes every step so no product is loop-invariant.
 constexpr int kFormChains = 8;
 
@@ -104,6 +106,30 @@ __global__ void imad_form_kernel(uint32_t* sink, int iters, uint32_t x, uint32_t
 #pragma unroll
     for (int c = 0; c < kFormChains; ++c) t ^= acc[c];
     if (t == 0x123456789ull) sink[threadIdx.x] = (uint32_t)t;
+  } else if constexpr (FORM == 4) {
+    static_assert(kFormChains == 8, "the add chain below is written for 8 words");
+    uint32_t acc[kFormChains];
+#pragma unroll
+    for (int c = 0; c < kFormChains; ++c) acc[c] = threadIdx.x * (c + 1);
+    for (int it = 0; it < iters; ++it) {
+      asm volatile(
+          "add.cc.u32 %0, %0, %8;\n\t"
+          "addc.cc.u32 %1, %1, %9;\n\t"
+          "addc.cc.u32 %2, %2, %10;\n\t"
+          "addc.cc.u32 %3, %3, %11;\n\t"
+          "addc.cc.u32 %4, %4, %12;\n\t"
+          "addc.cc.u32 %5, %5, %13;\n\t"
+          "addc.cc.u32 %6, %6, %14;\n\t"
+          "addc.u32 %7, %7, %15;"
+          : "+r"(acc[0]), "+r"(acc[1]), "+r"(acc[2]), "+r"(acc[3]), "+r"(acc[4]), "+r"(acc[5]), "+r"(acc[6]),
+            "+r"(acc[7])
+          : "r"(v[0] ^ u), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]));
+      u += 0x9E3779B9u;
+    }
+    uint32_t t = 0;
+#pragma unroll
+    for (int c = 0; c < kFormChains; ++c) t ^= acc[c];
+    if (t == 0x12345678u) sink[threadIdx.x] = t;
   } else {
     uint32_t acc[kFormChains];
 #pragma unroll
@@ -317,7 +343,7 @@ struct Coop {
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       row(acc, a, b[i]);
-      const uint32_t m = __shfl_sync(mask, acc[0] * P::PINV, 0, TPI);
+      const uint32_t m = __shfl_sync(mask, acc[0] * row_pinv<P>(), 0, TPI);
       row(acc, pl, m);
       uint32_t nxt = __shfl_down_sync(mask, acc[0], 1, TPI);
       if (lane == TPI - 1) nxt = 0u;
@@ -619,7 +645,8 @@ extern "C" int gsn_microbench_imad_form(int form, int iters, double* ops_per_s) 
     case 1: return run_imad_form<1>(iters, ops_per_s);
     case 2: return run_imad_form<2>(iters, ops_per_s);
     case 3: return run_imad_form<3>(iters, ops_per_s);
-    default: return set_error(GSN_ERR_ARG, "form must be 1 (mad.wide), 2 (mad.lo) or 3 (mad.hi)");
+    case 4: return run_imad_form<4>(iters, ops_per_s);
+    default: return set_error(GSN_ERR_ARG, "form must be 1 (mad.wide), 2 (mad.lo), 3 (mad.hi) or 4 (add.cc chain)");
   }
 }
 

@@ -92,7 +92,7 @@ __device__ __forceinline__ void reduce_wide(Fe<P>& x, const uint32_t (&T)[2 * P:
   t[2 * N + 1] = 0u;
 #pragma unroll
   for (int k = 0; k <= N; ++k) {
-    const uint32_t m = t[k] * P::PINV;
+    const uint32_t m = t[k] * row_pinv<P>();
     uint64_t c = 0;
 #pragma unroll
     for (int j = 0; j < N; ++j) {

@@ -26,7 +26,7 @@ def main() -> None:
     ap.add_argument("--batch", type=int, default=0, help="jobs in one batched launch (0: one transform)")
     ap.add_argument("--batch-lo", type=int, default=10)
     ap.add_argument("--batch-hi", type=int, default=18)
-    ap.add_argument("--microbench", default="", choices=["", "imad", "imad_wide", "imad_lo", "imad_hi"],
+    ap.add_argument("--microbench", default="", choices=["", "imad", "imad_wide", "imad_lo", "imad_hi", "add_chain"],
                     help="run one integer multiply-add microbenchmark instead (--iters steps per thread)")
     ap.add_argument("--iters", type=int, default=2000)
     ap.add_argument("--multiexp", type=int, default=0, help="log2 n: run gsn_multiexp on 2^n elements instead")
@@ -97,7 +97,7 @@ def run_microbench(g, args) -> None:
         g._lib.check(lib.gsn_microbench_imad(args.iters, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
         print(f"carry-chain multiply-adds: {a.value / 1e12:.3f} T/s, {b.value:.1f} per SM per clock at {c.value:.0f} MHz")
         return
-    form = {"imad_wide": 1, "imad_lo": 2, "imad_hi": 3}[args.microbench]
+    form = {"imad_wide": 1, "imad_lo": 2, "imad_hi": 3, "add_chain": 4}[args.microbench]
     v = ctypes.c_double()
     g._lib.check(lib.gsn_microbench_imad_form(form, args.iters, ctypes.byref(v)))
     print(f"{args.microbench}: {v.value / 1e12:.3f} T instructions/s")

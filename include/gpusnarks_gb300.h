@@ -365,7 +365,9 @@ uint64_t gsn_kernel_launch_count(void);
 int gsn_microbench_imad(int iters, double* mads_per_s, double* mads_per_clk_sm, double* sm_mhz);
 /* The multiply-add forms without the carry flag, on every SM at full
  * occupancy, independent accumulators per thread (no reference counterpart):
- * form 1 mad.wide.u32 (32x32->64 accumulate), 2 mad.lo.u32, 3 mad.hi.u32.
+ * form 1 mad.wide.u32 (32x32->64 accumulate), 2 mad.lo.u32, 3 mad.hi.u32;
+ * form 4 is an 8-word add.cc/addc.cc/addc chain, the carry-only adds of the
+ * products and of modular add/subtract (it runs on the ALU pipe).
  * Returns PTX instructions per second; compares the carry-chain rate of
  * gsn_microbench_imad with what the multiply pipe issues without carries. */
 int gsn_microbench_imad_form(int form, int iters, double* ops_per_s);
