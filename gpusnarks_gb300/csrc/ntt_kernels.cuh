@@ -35,6 +35,15 @@ __device__ __forceinline__ uint64_t tw_index(int tw_log, int log_n, int inverse,
   return idx;
 }
 
+// The same in 32 bits, for the per-element arithmetic of ntt_tile: every transform has at most 2^28 elements
+// (the fields' size limits), and so does every twiddle table.
+__device__ __forceinline__ uint32_t tw_index32(int tw_log, int log_n, int inverse, uint32_t e) {
+  const uint32_t size = 1u << tw_log;
+  uint32_t idx = e << (tw_log - log_n);
+  if (inverse) idx = (size - idx) & (size - 1u);
+  return idx;
+}
+
 template <class P>
 __device__ __forceinline__ void tw_load(Fe<P>& w, const uint32_t* tw, uint64_t idx) {
   fe_load<P>(w, tw + idx * P::N);
@@ -63,6 +72,8 @@ __device__ __forceinline__ uint64_t rest_offset(uint64_t rest, int npass, const 
 // (twiddle, pre- or post-table entry) from memory row by row (fe_mul_mem) instead of loading it into registers
 // first; A must then live in addressable memory (a __grid_constant__ parameter or shared memory), since the
 // pre-scale constant is read through a pointer to A.pre_const.
+// Element positions and twiddle exponents are 32-bit (at most 2^28 elements per transform): 64-bit index
+// arithmetic per butterfly takes multiply-pipe instructions from the products.
 template <class P, bool TW_MEM>
 __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
   constexpr int N = P::N;
@@ -71,31 +82,32 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
   const int tid = threadIdx.x, nthr = blockDim.x;
 
   // --- tile geometry -------------------------------------------------------
-  uint64_t base = 0;     // non-last: first element of the tile
-  uint64_t jbase = 0;    // non-last: first suffix index j'
-  uint64_t rowpre = 0;   // last: prefix_lin of row 0 = (k0_first << (outer_log - lo0)) + rest
-  uint64_t obase = 0;    // last: output offset of row 0 (k_0 = k0_first, k = 0)
+  uint32_t base = 0;     // non-last: first element of the tile
+  uint32_t jbase = 0;    // non-last: first suffix index j'
+  uint32_t rowpre = 0;   // last: prefix_lin of row 0 = (k0_first << (outer_log - lo0)) + rest
+  uint32_t obase = 0;    // last: output offset of row 0 (k_0 = k0_first, k = 0)
   int lo0 = 0;           // last: log2 n_0 (0 for a single pass)
+  const uint32_t t32 = (uint32_t)tile;  // tiles < 2^28
   if (!A.last) {
     const int per_prefix_log = A.log_inner - lj;
-    const uint64_t prefix = tile >> per_prefix_log;
-    const uint64_t jb = tile & (((uint64_t)1 << per_prefix_log) - 1);
+    const uint32_t prefix = t32 >> per_prefix_log;
+    const uint32_t jb = t32 & ((1u << per_prefix_log) - 1u);
     jbase = jb << lj;
     base = (prefix << (lr + A.log_inner)) + jbase;
   } else {
     lo0 = (A.npass == 1) ? 0 : A.radix_log[0];
     const int k0b_log = lo0 - lj;
-    const uint64_t k0b = tile & (((uint64_t)1 << k0b_log) - 1);
-    const uint64_t rest = tile >> k0b_log;
-    const uint64_t k0 = k0b << lj;
+    const uint32_t k0b = t32 & ((1u << k0b_log) - 1u);
+    const uint32_t rest = t32 >> k0b_log;
+    const uint32_t k0 = k0b << lj;
     rowpre = (k0 << (A.log_outer - lo0)) + rest;
-    obase = k0 + (rest_offset(rest, A.npass, A.radix_log) << lo0);
+    obase = k0 + ((uint32_t)rest_offset(rest, A.npass, A.radix_log) << lo0);
   }
 
   // global position of tile element (k, jj) in the source array
-  auto src_pos = [&](int k, int jj) -> uint64_t {
-    return !A.last ? base + ((uint64_t)k << A.log_inner) + jj
-                   : ((rowpre + ((uint64_t)jj << (A.log_outer - lo0))) << lr) + k;
+  auto src_pos = [&](int k, int jj) -> uint32_t {
+    return !A.last ? base + ((uint32_t)k << A.log_inner) + (uint32_t)jj
+                   : ((rowpre + ((uint32_t)jj << (A.log_outer - lo0))) << lr) + (uint32_t)k;
   };
 
   // --- load (no arithmetic) ------------------------------------------------
@@ -109,7 +121,7 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
       k = e & (R - 1);
     }
     Fe<P> x;
-    fe_load_cg<P>(x, A.src + src_pos(k, jj) * N);
+    fe_load_cg<P>(x, A.src + (size_t)src_pos(k, jj) * N);
     fe_store<P>(sm + ((k << lj) + jj) * N, x);
   }
   __syncthreads();
@@ -141,7 +153,7 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
         out = sm + ((k << lj) + jj) * N;
         fe_load<P>(x, out);
         if (A.pre_table) {
-          take(A.pre_table + src_pos(k, jj) * N);
+          take(A.pre_table + (size_t)src_pos(k, jj) * N);
         } else if constexpr (TW_MEM) {
           take(A.pre_const);
         } else {
@@ -168,20 +180,20 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
         fe_store<P>(sm + ((u << lj) + jj) * N, sum);
         out = sm + ((v << lj) + jj) * N;
         if (i != 0) {
-          const uint64_t e = ((uint64_t)i << ph) << (A.log_n - lr);
-          take(A.tw + tw_index(A.tw_log, A.log_n, A.inverse, e) * N);
+          const uint32_t e = (uint32_t)i << (ph + A.log_n - lr);
+          take(A.tw + (size_t)tw_index32(A.tw_log, A.log_n, A.inverse, e) * N);
         }
       } else {
         const int k = b >> lj, jj = b & (J - 1);
         fe_load<P>(x, sm + ((bitrev_bits((uint32_t)k, lr) << lj) + jj) * N);
         if (!A.last) {
-          const uint64_t ex = ((jbase + jj) * (uint64_t)k) << A.log_outer;
-          out = A.dst + (base + ((uint64_t)k << A.log_inner) + jj) * N;
-          if (ex != 0) take(A.tw + tw_index(A.tw_log, A.log_n, A.inverse, ex) * N);
+          const uint32_t ex = ((jbase + (uint32_t)jj) * (uint32_t)k) << A.log_outer;  // < n
+          out = A.dst + (size_t)(base + ((uint32_t)k << A.log_inner) + (uint32_t)jj) * N;
+          if (ex != 0) take(A.tw + (size_t)tw_index32(A.tw_log, A.log_n, A.inverse, ex) * N);
         } else {
-          const uint64_t opos = obase + jj + ((uint64_t)k << A.log_outer);
-          out = A.dst + opos * N;
-          if (A.post_table) take(A.post_table + opos * N);
+          const uint32_t opos = obase + (uint32_t)jj + ((uint32_t)k << A.log_outer);
+          out = A.dst + (size_t)opos * N;
+          if (A.post_table) take(A.post_table + (size_t)opos * N);
         }
       }
       if (mul) {
