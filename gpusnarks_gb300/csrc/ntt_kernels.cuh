@@ -217,6 +217,8 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
 //   multiplier in registers, cap 102 (4 CTAs, 48 bytes of spills):  0.3783 / 1.4354 / 5.988
 //   multiplier in registers, cap 96  (5 CTAs, 112 bytes of spills): 0.3707 / 1.4383 / 6.043
 //   multiplier from memory,  cap 96  (5 CTAs, no spills):            0.3654 / 1.4172 / 6.040
+// With the tile's 32-bit index arithmetic ptxas spills 12 bytes at the same cap; 2^18 / 2^20 ran in 0.3672 /
+// 1.4176 ms against 0.3659 / 1.4184 before it.
 template <class P>
 __host__ __device__ constexpr bool pass_tw_mem() {
   return P::N >= 16;
