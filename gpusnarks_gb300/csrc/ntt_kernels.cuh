@@ -129,10 +129,13 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
   // --- phases; every multiplication goes through the single product below, so
   // the fully unrolled product exists once in the instruction stream --------
   //   ph = -1        pre-scale (first pass: coset powers or n^-1)
-  //   ph = 0..lr-1   radix-2 DIF stage ph (natural in, bit-reversed out)
-  //   ph = lr        four-step twiddle (non-last) or post table (last), store
+  //   ph = 0..lr-2   radix-2 DIF stage ph (natural in, bit-reversed out)
+  //   ph = lr        the last stage (ph = lr-1, twiddle 1: each output row is the sum or the difference of two
+  //                  rows, no product) fused with the four-step twiddle (non-last) or post table (last) and the
+  //                  store.  That saves one barrier and one shared-memory store of the tile per pass.
   const bool pre = A.first && (A.pre_table || A.has_pre_const);
   for (int ph = pre ? -1 : 0; ph <= lr; ++ph) {
+    if (lr > 0 && ph == lr - 1) continue;  // fused into ph = lr; uniform across the block
     const bool stage = ph >= 0 && ph < lr;
     const int count = stage ? (R >> 1) * J : R * J;
     for (int b = tid; b < count; b += nthr) {
@@ -185,7 +188,20 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
         }
       } else {
         const int k = b >> lj, jj = b & (J - 1);
-        fe_load<P>(x, sm + ((bitrev_bits((uint32_t)k, lr) << lj) + jj) * N);
+        if (lr > 0) {
+          // row r = bitrev(k) after the last stage: the sum (r even) or difference (r odd) of rows r&~1, r|1
+          const uint32_t r = bitrev_bits((uint32_t)k, lr);
+          Fe<P> y;
+          fe_load<P>(x, sm + (((r & ~1u) << lj) + jj) * N);
+          fe_load<P>(y, sm + (((r | 1u) << lj) + jj) * N);
+          if (r & 1u) {
+            fe_sub<P>(x, x, y);
+          } else {
+            fe_add<P>(x, x, y);
+          }
+        } else {
+          fe_load<P>(x, sm + jj * N);
+        }
         if (!A.last) {
           const uint32_t ex = ((jbase + (uint32_t)jj) * (uint32_t)k) << A.log_outer;  // < n
           out = A.dst + (size_t)(base + ((uint32_t)k << A.log_inner) + (uint32_t)jj) * N;
