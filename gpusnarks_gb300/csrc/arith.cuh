@@ -169,7 +169,7 @@ __device__ __forceinline__ void fe_sub(Fe<P>& r, const Fe<P>& a, const Fe<P>& b)
 // There the factor is read from constant memory, whose contents the compiler does not assume; every
 // other field keeps the immediate.
 template <class P>
-__constant__ uint32_t c_row_pinv = P::PINV;
+static __constant__ uint32_t c_row_pinv = P::PINV;
 
 template <class P>
 __device__ __forceinline__ uint32_t row_pinv() {

@@ -111,20 +111,28 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
   };
 
   // --- load (no arithmetic) ------------------------------------------------
-  for (int e = tid; e < R * J; e += nthr) {
-    int k, jj;
-    if (!A.last) {
-      k = e >> lj;
-      jj = e & (J - 1);
-    } else {
-      jj = e >> lr;  // input rows are contiguous on the last pass
-      k = e & (R - 1);
+  // Multi-limb fields without a pre-scale: stage 0 reads its two rows from global memory itself, one barrier and
+  // one shared-memory store of the tile fewer (MNT4 and BLS transforms 1-2.4% faster on GB300).  Its product hides
+  // the load latency.  The 32-bit field keeps the load phase, whose many loads in flight its short butterflies
+  // need (a p32 batch ran 6.8% slower with stage-0 loads).
+  const bool pre = A.first && (A.pre_table || A.has_pre_const);
+  const bool load_in_stage0 = N >= 8 && !pre && lr >= 2;
+  if (!load_in_stage0) {
+    for (int e = tid; e < R * J; e += nthr) {
+      int k, jj;
+      if (!A.last) {
+        k = e >> lj;
+        jj = e & (J - 1);
+      } else {
+        jj = e >> lr;  // input rows are contiguous on the last pass
+        k = e & (R - 1);
+      }
+      Fe<P> x;
+      fe_load_cg<P>(x, A.src + (size_t)src_pos(k, jj) * N);
+      fe_store<P>(sm + ((k << lj) + jj) * N, x);
     }
-    Fe<P> x;
-    fe_load_cg<P>(x, A.src + (size_t)src_pos(k, jj) * N);
-    fe_store<P>(sm + ((k << lj) + jj) * N, x);
+    __syncthreads();
   }
-  __syncthreads();
 
   // --- phases; every multiplication goes through the single product below, so
   // the fully unrolled product exists once in the instruction stream --------
@@ -133,7 +141,6 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
   //   ph = lr        the last stage (ph = lr-1, twiddle 1: each output row is the sum or the difference of two
   //                  rows, no product) fused with the four-step twiddle (non-last) or post table (last) and the
   //                  store.  That saves one barrier and one shared-memory store of the tile per pass.
-  const bool pre = A.first && (A.pre_table || A.has_pre_const);
   for (int ph = pre ? -1 : 0; ph <= lr; ++ph) {
     if (lr > 0 && ph == lr - 1) continue;  // fused into ph = lr; uniform across the block
     const bool stage = ph >= 0 && ph < lr;
@@ -176,8 +183,13 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
         const int u = (group << (log_half + 1)) + i;
         const int v = u + (1 << log_half);
         Fe<P> y, sum;
-        fe_load<P>(x, sm + ((u << lj) + jj) * N);
-        fe_load<P>(y, sm + ((v << lj) + jj) * N);
+        if (ph == 0 && load_in_stage0) {
+          fe_load_cg<P>(x, A.src + (size_t)src_pos(u, jj) * N);
+          fe_load_cg<P>(y, A.src + (size_t)src_pos(v, jj) * N);
+        } else {
+          fe_load<P>(x, sm + ((u << lj) + jj) * N);
+          fe_load<P>(y, sm + ((v << lj) + jj) * N);
+        }
         fe_add<P>(sum, x, y);
         fe_sub<P>(x, x, y);
         fe_store<P>(sm + ((u << lj) + jj) * N, sum);
@@ -233,8 +245,7 @@ __device__ void ntt_tile(const PassArgs& A, uint64_t tile, uint32_t* sm) {
 //   multiplier in registers, cap 102 (4 CTAs, 48 bytes of spills):  0.3783 / 1.4354 / 5.988
 //   multiplier in registers, cap 96  (5 CTAs, 112 bytes of spills): 0.3707 / 1.4383 / 6.043
 //   multiplier from memory,  cap 96  (5 CTAs, no spills):            0.3654 / 1.4172 / 6.040
-// With the tile's 32-bit index arithmetic ptxas spills 12 bytes at the same cap; 2^18 / 2^20 ran in 0.3672 /
-// 1.4176 ms against 0.3659 / 1.4184 before it.
+// The tile's later changes (32-bit indices, fused last stage, stage-0 loads) leave it at 94 registers, no spills.
 template <class P>
 __host__ __device__ constexpr bool pass_tw_mem() {
   return P::N >= 16;
