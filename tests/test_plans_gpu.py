@@ -99,3 +99,44 @@ def test_rb_plans_match_committed_plans(gsn, cuda_device, tmp_path, k, radix):
         assert torch.equal(y, want[gsn.FORWARD])
     finally:
         _restore(gsn)
+
+
+def generic_plan(fid, log_n, radix, lj, block):
+    """A plan for the generic tile (kernel 0) with the tile widths make_split_plan gives (runtime.cu)."""
+    npass = len(radix)
+    log_j = []
+    for i, r in enumerate(radix):
+        last = i == npass - 1
+        inner = sum(radix[i + 1:])
+        log_j.append((0 if npass == 1 else min(lj, radix[0])) if last else min(lj, inner))
+    pad = lambda v: v + [0] * (4 - len(v))
+    return {"field": fid, "mode": 0, "log_n": log_n, "kernel": 0, "e_log": 4, "npass": npass,
+            "radix_log": pad(list(radix)), "log_j": pad(log_j), "block": pad([block] * npass), "ms": 1.0}
+
+
+# Passes of radix 2^1 (the fused last stage is the tile's only stage), 2^2 (the smallest tile whose stage 0
+# reads global memory) and larger, in every position of the pass sequence.
+GENERIC_SMALL = [(2, [1, 1]), (3, [1, 2]), (3, [2, 1]), (4, [2, 2]), (5, [2, 3]), (5, [1, 1, 3]), (6, [1, 2, 3]),
+                 (7, [3, 4]), (9, [3, 3, 3]), (9, [2, 5, 2])]
+
+
+@pytest.mark.parametrize("fname", ["p32", "bls12_381_fr", "mnt4753_fr"])
+@pytest.mark.parametrize("lj,block", [(0, 32), (1, 64), (2, 32)])
+def test_generic_small_radix_plans_match_oracle(gsn, cuda_device, tmp_path, fname, lj, block):
+    f = gsn.FIELDS[fname]
+    try:
+        for k, radix in GENERIC_SMALL:  # one plan per size in a table, so one table per case
+            _use(gsn, tmp_path, [generic_plan(f.fid, k, radix, lj, block)])
+            p = gsn.plan(f, k)
+            assert p["kernel"] == 0 and p["radix_log"][:len(radix)] == radix, (k, radix, p)
+            x = f.random_array(1 << k, seed=0x5EED1200 + 16 * k + 4 * lj + f.fid)
+            for direction in (gsn.FORWARD, gsn.INVERSE, gsn.COSET_FORWARD, gsn.COSET_INVERSE):
+                y = gsn.to_device(x)
+                gsn.ntt(f, y, direction=direction)
+                want = {gsn.FORWARD: lambda: O.ntt(f.fid, x),
+                        gsn.INVERSE: lambda: O.intt(f.fid, x),
+                        gsn.COSET_FORWARD: lambda: O.coset_ntt(f.fid, x, O.GENERATORS[f.fid]),
+                        gsn.COSET_INVERSE: lambda: O.coset_intt(f.fid, x, O.GENERATORS[f.fid])}[direction]()
+                assert np.array_equal(gsn.to_host(y).reshape(x.shape), want.reshape(x.shape)), (k, radix, direction)
+    finally:
+        _restore(gsn)
